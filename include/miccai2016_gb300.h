@@ -1,0 +1,112 @@
+/*
+ * miccai2016_gb300.h -- C ABI of the GB300 tubular-segmentation kernels.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int status (M16_OK = 0) and never throws.  Unless a comment says "host",
+ * pointers are CUDA device pointers owned by the caller.  Scratch memory comes
+ * from a caller-provided workspace whose size the matching *_workspace_bytes()
+ * function reports; the library itself calls no allocator.  `stream` is a
+ * cudaStream_t passed as void*; all work is enqueued on it.
+ *
+ * Volumes are C-ordered float32 arrays of shape (d0, d1, d2) with d2 the
+ * fastest axis, exactly the numpy layout the reference's Python modules take.
+ * Squeezed quaternions are (d0, d1, d2, 3) interleaved triples as produced by
+ * the reference's qsqueeze() (src/clcode/quaternion_math.h:20-39).
+ *
+ * Each declaration cites the reference interface it replaces.
+ */
+#ifndef MICCAI2016_GB300_H
+#define MICCAI2016_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define M16_OK 0
+#define M16_ERR_BAD_SHAPE 1     /* a dimension is < 1, or the volume is too large */
+#define M16_ERR_BAD_ARG 2       /* a NULL pointer, a non-finite or out-of-range parameter */
+#define M16_ERR_WORKSPACE 3     /* workspace NULL, misaligned or smaller than required */
+#define M16_ERR_CUDA 4          /* a CUDA runtime call failed */
+#define M16_ERR_TIMEOUT 5       /* a bounded device-side wait gave up */
+
+/* Human-readable name of a status code (static string). */
+const char *m16_status_string(int status);
+
+/* Version of this ABI; bumped on any incompatible change. */
+int m16_abi_version(void);
+
+/* ---- continuous max-flow with anisotropic TV ------------------------------
+ * Replaces CmfCutQAnisotropicGpu.CutParameters
+ * (src/processing/continuous_cut_anisotropic_gpu.py:38-49).               */
+typedef struct m16_cut_params {
+    double cc;          /* augmented-Lagrangian step (CutParameters.cc, 0.2) */
+    double steps;       /* gradient-ascent step (CutParameters.steps, 0.11) */
+    double error_bound; /* stop when the residual falls below (CutParameters.error_bound) */
+    int32_t num_iter;   /* maximum number of iterations (CutParameters.num_iter) */
+    int32_t update;     /* check the residual every `update` iterations (>= 1) */
+    double scaling[3];  /* voxel size [mm/voxel] per axis, the `scaling` argument */
+} m16_cut_params;
+
+/* Workspace bytes m16_maxflow_solve needs for a (d0, d1, d2) volume. */
+size_t m16_maxflow_workspace_bytes(int32_t d0, int32_t d1, int32_t d2, const m16_cut_params *params);
+
+/*
+ * One continuous max-flow solve (paper Alg. 1.1), replacing
+ * CmfCutQAnisotropicGpu.execute(img, quats, eigs, alpha, cs, ct, labels, scaling)
+ * (src/processing/continuous_cut_anisotropic_gpu.py:143-344) and its kernels
+ * update_p / update_u / update_tmp (src/clcode-anisotropic/update_qp.cl:150-316).
+ *
+ *   img        N      image; u starts as img / (max(img) + FLT_MIN)
+ *   quat3      N x 3  squeezed quaternions of the anisotropy's eigenvectors
+ *   sqevals3   host, 3 doubles: square roots of constant eigenvalues, or NULL
+ *   sqeigs     N x 3  per-voxel square roots of the eigenvalues (when sqevals3 == NULL)
+ *   alpha      N      TV weight per voxel, or NULL to use alpha_scalar everywhere
+ *   cs, ct     N      source / sink capacities
+ *   labels     N      uint8 seeds (1 foreground, 2 background) for the supervised
+ *                     variant, or NULL for the unsupervised cut
+ *   u          N      output: the relaxed labelling (not clipped to [0, 1])
+ *   iterations host   output: iterations run (the reference's loop counter + 1 at a break)
+ *   residuals  host   optional: the residual of every check, up to residuals_cap values;
+ *                     n_residuals (host, optional) receives how many were checked
+ *
+ * The residual is cc * mean|div(hp) - p_s + p_t| checked before the u-update of
+ * every iteration i with i % update == 0; the solve stops at the first check
+ * that is NaN or below error_bound, exactly as the reference's loop does.
+ * The call returns after the solve completed on `stream` (it synchronizes
+ * `stream` to read the stopping state); it never synchronizes the device.
+ */
+int m16_maxflow_solve(const float *img, const float *quat3, const double *sqevals3,
+                      const float *sqeigs, const float *alpha, float alpha_scalar,
+                      const float *cs, const float *ct, const uint8_t *labels,
+                      int32_t d0, int32_t d1, int32_t d2, const m16_cut_params *params,
+                      float *u, int32_t *iterations, double *residuals, int32_t residuals_cap,
+                      int32_t *n_residuals, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Counters of one solve, for benchmarks and tracing. */
+typedef struct m16_solve_stats {
+    int32_t time_kernels;  /* in: 1 brackets every flow/label kernel launch with CUDA events */
+    int32_t launches;      /* out: kernels the call launched */
+    int32_t p_launches;    /* out: flow (P) kernel launches that ran */
+    int32_t u_launches;    /* out: label (U) kernel launches that ran */
+    double p_ms;           /* out: summed device time of the P launches (time_kernels only) */
+    double u_ms;           /* out: summed device time of the U launches (time_kernels only) */
+} m16_solve_stats;
+
+/* m16_maxflow_solve with counters; stats (host) may be NULL. */
+int m16_maxflow_solve_ex(const float *img, const float *quat3, const double *sqevals3,
+                         const float *sqeigs, const float *alpha, float alpha_scalar,
+                         const float *cs, const float *ct, const uint8_t *labels,
+                         int32_t d0, int32_t d1, int32_t d2, const m16_cut_params *params,
+                         float *u, int32_t *iterations, double *residuals, int32_t residuals_cap,
+                         int32_t *n_residuals, void *workspace, size_t workspace_bytes, void *stream,
+                         m16_solve_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MICCAI2016_GB300_H */

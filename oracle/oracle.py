@@ -1,0 +1,216 @@
+"""
+oracle/oracle.py -- numpy front end of the CPU checker.
+
+TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the CPU
+baseline legs of bench.py import this module; the product package never does.
+
+Two libraries sit behind it:
+* liboracle.so -- the C restatement in oracle/*.c (the "port"), built
+  everywhere, including on machines without the reference checkout;
+* libref.so    -- the reference's own OpenCL C kernels compiled through
+  oracle/ref_shim (only where the reference checkout exists).  It is used to
+  pin the port and to generate the committed golden fixtures.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+_u16p = np.ctypeslib.ndpointer(dtype=np.uint16, flags="C_CONTIGUOUS")
+_i64 = ctypes.c_int64
+_vp = ctypes.c_void_p
+
+_lib = None
+_ref = None
+
+
+def lib():
+    """The C restatement (liboracle.so), built on first use."""
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        _lib = ctypes.CDLL(path)
+        _declare_oracle(_lib)
+    return _lib
+
+
+def ref():
+    """The reference kernels through the shim (libref.so), or None."""
+    global _ref
+    if _ref is None:
+        path = _build.ref_lib_path()
+        if not os.path.exists(path):
+            path = _build.build_ref()
+        if path is None or not os.path.exists(path):
+            return None
+        _ref = ctypes.CDLL(path)
+    return _ref
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_vp)
+
+
+def _f32(a):
+    return np.require(a, dtype=np.float32, requirements=["C", "A"])
+
+
+def _declare_oracle(L):
+    L.oracle_maxflow_solve.restype = ctypes.c_int
+    L.oracle_maxflow_solve.argtypes = [_vp] * 8 + [_i64, _i64, _i64, _vp, ctypes.c_double,
+                                                   ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_double, _vp, _vp, _vp]
+    L.oracle_sum_abs.restype = ctypes.c_double
+    L.oracle_sum_abs.argtypes = [_vp, _i64]
+    L.oracle_mf_update_p.restype = None
+    L.oracle_mf_update_p.argtypes = [_i64, _i64, _i64, _vp, ctypes.c_double, ctypes.c_double, _vp] + [_vp] * 7
+    L.oracle_mf_update_u.restype = None
+    L.oracle_mf_update_u.argtypes = [_i64, _i64, _i64, _vp, ctypes.c_double, ctypes.c_double] + [_vp] * 9
+    L.oracle_mf_update_tmp.restype = None
+    L.oracle_mf_update_tmp.argtypes = [_i64, _vp, ctypes.c_double, _vp, _vp]
+
+
+# ----------------------------------------------------------------------------
+# max-flow
+# ----------------------------------------------------------------------------
+
+def mf_consts(scaling=(1, 1, 1), cc=0.2, steps=0.11, sqevals=(1.0, 1.0, 1.0)):
+    """RCC, RS0-2, SS0-2, SQEVAL0-2 as the reference derives them
+    (src/processing/continuous_cut_anisotropic_gpu.py:104-129)."""
+    scaling = np.asarray(scaling, dtype=np.float64)
+    rs = 1.0 / scaling
+    smin = np.min(scaling)
+    ss = steps / scaling * smin ** 2
+    rcc = 1.0 / (cc * smin ** 2)
+    return np.array([rcc, rs[0], rs[1], rs[2], ss[0], ss[1], ss[2],
+                     sqevals[0], sqevals[1], sqevals[2]], dtype=np.float64)
+
+
+def _split_eigs(eigs, shape):
+    """sqrt of a constant 3-tuple or of a per-voxel (z,y,x,3) array, as
+    continuous_cut_anisotropic_gpu.py:216-221 and 246-251 arrange them."""
+    sq = np.sqrt(np.asanyarray(eigs))
+    if sq.ndim == 1:
+        return np.ascontiguousarray(sq, dtype=np.float64), None
+    return None, _f32(sq.reshape(-1, 3))
+
+
+def maxflow_solve(img, quats, eigs, alpha, cs, ct, labels=None, scaling=None, cc=0.2, steps=0.11,
+                  num_iter=1000, update=1, error_bound=1e-4):
+    """One CmfCutQAnisotropicGpu.execute() solve on the CPU.
+
+    Returns (u, iterations, residuals) where residuals lists every checked
+    value of cc * mean|div(hp) - p_s + p_t|."""
+    img = _f32(img)
+    shape = img.shape
+    n = img.size
+    sqc, sqp = _split_eigs(eigs, shape)
+    if not isinstance(alpha, np.ndarray):
+        alpha = np.multiply(alpha, np.ones(shape), dtype=np.float32)
+    alpha = _f32(alpha)
+    cs, ct = _f32(cs), _f32(ct)
+    q = _f32(quats).reshape(-1, 3)
+    lab = None if labels is None else np.require(labels, dtype=np.uint8, requirements=["C", "A"])
+    sc = np.asarray((1, 1, 1) if scaling is None else scaling, dtype=np.float64)
+    u = np.empty(shape, np.float32)
+    n_checks = ctypes.c_int(0)
+    max_checks = (num_iter // max(update, 1)) + 2
+    resid = np.zeros(max_checks, np.float64)
+    iters = lib().oracle_maxflow_solve(_ptr(img), _ptr(q), None if sqc is None else _ptr(sqc), _ptr(sqp),
+                                       _ptr(alpha), _ptr(cs), _ptr(ct), _ptr(lab), shape[0], shape[1],
+                                       shape[2], _ptr(sc), cc, steps, num_iter, update, error_bound,
+                                       _ptr(u), _ptr(resid), ctypes.byref(n_checks))
+    return u, int(iters), resid[:n_checks.value].copy()
+
+
+def sum_abs(x):
+    x = _f32(x).ravel()
+    return float(lib().oracle_sum_abs(_ptr(x), x.size))
+
+
+def mf_update_p(hp, tmp, quats, eigs, alpha, scaling=(1, 1, 1), cc=0.2, steps=0.11):
+    """In-place update_p on hp = [hp0, hp1, hp2] (each (z,y,x) float32)."""
+    shape = tmp.shape
+    sqc, sqp = _split_eigs(eigs, shape)
+    sc = np.asarray(scaling, dtype=np.float64)
+    lib().oracle_mf_update_p(shape[0], shape[1], shape[2], _ptr(sc), cc, steps,
+                             None if sqc is None else _ptr(sqc), _ptr(hp[0]), _ptr(hp[1]), _ptr(hp[2]),
+                             _ptr(_f32(tmp)), _ptr(_f32(quats)), _ptr(sqp), _ptr(_f32(alpha)))
+
+
+def mf_update_u(hp, tmp, cs, ct, pt, u, labels=None, scaling=(1, 1, 1), cc=0.2, steps=0.11):
+    shape = tmp.shape
+    sc = np.asarray(scaling, dtype=np.float64)
+    lab = None if labels is None else np.require(labels, dtype=np.uint8, requirements=["C", "A"])
+    lib().oracle_mf_update_u(shape[0], shape[1], shape[2], _ptr(sc), cc, steps, _ptr(hp[0]), _ptr(hp[1]),
+                             _ptr(hp[2]), _ptr(tmp), _ptr(_f32(cs)), _ptr(_f32(ct)), _ptr(pt), _ptr(u),
+                             _ptr(lab))
+
+
+def mf_update_tmp(tmp, u, scaling=(1, 1, 1), cc=0.2):
+    sc = np.asarray(scaling, dtype=np.float64)
+    lib().oracle_mf_update_tmp(tmp.size, _ptr(sc), cc, _ptr(tmp), _ptr(_f32(u)))
+
+
+# --- the same, through the reference kernels ----------------------------------
+
+def ref_mf_kernels(const_evals: bool, supervised: bool):
+    """(update_p, update_u, update_tmp) of the shim-compiled update_qp.cl."""
+    R = ref()
+    if R is None:
+        return None
+    suf = ("_c" if const_evals else "_p") + ("_s" if supervised else "_u")
+    return (getattr(R, "ref_update_p" + suf), getattr(R, "ref_update_u" + suf),
+            getattr(R, "ref_update_tmp" + suf))
+
+
+def ref_maxflow_solve(img, quats, eigs, alpha, cs, ct, labels=None, scaling=None, cc=0.2, steps=0.11,
+                      num_iter=1000, update=1, error_bound=1e-4):
+    """The reference's solve loop (continuous_cut_anisotropic_gpu.py:198-344)
+    driving the reference's own kernels; the residual uses the port's
+    sum_abs.  Returns (u, iterations, residuals)."""
+    img = _f32(img)
+    shape = img.shape
+    n = img.size
+    sq = np.sqrt(np.asanyarray(eigs))
+    const = sq.ndim == 1
+    kp, ku, kt = ref_mf_kernels(const, labels is not None)
+    sc = (1, 1, 1) if scaling is None else scaling
+    k = mf_consts(sc, cc, steps, sq if const else (1.0, 1.0, 1.0))
+    if not isinstance(alpha, np.ndarray):
+        alpha = np.multiply(alpha, np.ones(shape), dtype=np.float32)
+    alpha, cs, ct = _f32(alpha), _f32(cs), _f32(ct)
+    if const:
+        e = _f32(quats)
+    else:
+        e = np.empty(shape + (6,), np.float32)
+        e[..., :3] = sq
+        e[..., 3:] = quats
+    lab = None if labels is None else np.require(labels, dtype=np.uint8, requirements=["C", "A"])
+    hp = [np.zeros(shape, np.float32) for _ in range(3)]
+    pt = np.fmin(cs, ct)
+    u = np.require(np.divide(img, np.max(img) + np.finfo(img.dtype).tiny), dtype=np.float32,
+                   requirements=["C", "A"])
+    tmp = np.zeros(shape, np.float32)
+    d0, d1, d2 = shape
+    kt(ctypes.c_long(n), _ptr(k), _ptr(tmp), _ptr(u))
+    resid = []
+    it = 0
+    for it in range(num_iter):
+        kp(d0, d1, d2, _ptr(k), _ptr(hp[0]), _ptr(hp[1]), _ptr(hp[2]), _ptr(tmp), _ptr(e), _ptr(alpha))
+        ku(d0, d1, d2, _ptr(k), _ptr(hp[0]), _ptr(hp[1]), _ptr(hp[2]), _ptr(tmp), _ptr(cs), _ptr(ct),
+           _ptr(pt), _ptr(u), _ptr(lab))
+        if update > 0 and not it % update:
+            err = sum_abs(tmp) / (n * k[0])
+            resid.append(err)
+            if np.isnan(err) or err < error_bound:
+                return u, it + 1, np.array(resid)
+        kt(ctypes.c_long(n), _ptr(k), _ptr(tmp), _ptr(u))
+    return u, num_iter, np.array(resid)

@@ -1,0 +1,55 @@
+"""
+Seeded inputs of the golden fixtures.  numpy's RandomState stream is the same
+on every platform, so the fixtures store only outputs; the inputs are rebuilt
+from these functions (tests/golden/make_golden.py writes the outputs).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def random_squeezed(rng, shape):
+    """Squeezed quaternions (phi, theta, psi) with uniform angles."""
+    return np.stack([rng.uniform(-np.pi, np.pi, shape), rng.uniform(0, np.pi, shape),
+                     rng.uniform(-np.pi, np.pi, shape)], -1).astype(np.float32)
+
+
+def maxflow_case(name):
+    """(inputs dict, solver kwargs) of one max-flow fixture."""
+    if name == "mf_const_unsup":
+        rng = np.random.RandomState(11)
+        shape = (20, 24, 28)
+        eigs = (1.0, 10 ** -1.5, 10 ** -1.5)
+        labels = None
+        scaling = (1, 1, 1)
+        kw = dict(num_iter=60, update=10, error_bound=-1.0)
+    elif name == "mf_point_sup":
+        rng = np.random.RandomState(12)
+        shape = (17, 10, 33)
+        eigs = None
+        labels = "random"
+        scaling = (1.5, 0.7, 1.2)
+        kw = dict(num_iter=45, update=7, error_bound=-1.0)
+    elif name == "mf_stop":
+        rng = np.random.RandomState(13)
+        shape = (16, 16, 16)
+        eigs = (1.0, 1.0, 1.0)
+        labels = None
+        scaling = (1, 1, 1)
+        kw = dict(num_iter=400, update=5, error_bound=2e-3)
+    else:
+        raise KeyError(name)
+    img = rng.normal(0.5, 0.5, shape).astype(np.float32)
+    quats = random_squeezed(rng, shape)
+    alpha = rng.uniform(0.01, 0.5, shape).astype(np.float32)
+    cs = rng.uniform(0, 1, shape).astype(np.float32)
+    ct = rng.uniform(0, 1, shape).astype(np.float32)
+    if eigs is None:
+        eigs = rng.uniform(0.01, 2.0, shape + (3,))
+    if labels == "random":
+        labels = rng.randint(0, 3, shape).astype(np.uint8)
+    inputs = dict(img=img, quats=quats, eigs=eigs, alpha=alpha, cs=cs, ct=ct, labels=labels, scaling=scaling)
+    return inputs, kw
+
+
+MAXFLOW_CASES = ("mf_const_unsup", "mf_point_sup", "mf_stop")

@@ -1,0 +1,36 @@
+"""
+Generates the golden fixtures in tests/golden/*.npz by running the reference's
+own OpenCL C kernels (compiled for the CPU through oracle/ref_shim; needs the
+reference checkout) on the seeded inputs of tests/golden/inputs.py.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, HERE)
+
+from oracle import oracle as O  # noqa: E402
+import inputs as I  # noqa: E402
+
+
+def make_maxflow():
+    for name in I.MAXFLOW_CASES:
+        inp, kw = I.maxflow_case(name)
+        u, iters, resid = O.ref_maxflow_solve(inp["img"], inp["quats"], inp["eigs"], inp["alpha"], inp["cs"],
+                                              inp["ct"], labels=inp["labels"], scaling=inp["scaling"], **kw)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, u=u, iterations=np.int64(iters), residuals=np.asarray(resid, np.float64))
+        print(name, u.shape, iters, len(resid), os.path.getsize(path))
+
+
+if __name__ == "__main__":
+    if O.ref() is None:
+        raise SystemExit("the reference checkout is needed to generate fixtures")
+    make_maxflow()

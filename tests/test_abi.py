@@ -1,0 +1,78 @@
+"""The C-ABI library builds, loads without a GPU and exports every function
+declared in include/*.h; argument validation that needs no GPU."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(m16_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from miccai2016_gb300 import _native
+    return _native.lib()
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert "m16_maxflow_solve" in names and len(names) >= 4
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in _declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_status_strings(lib):
+    from miccai2016_gb300 import _native as N
+    assert N.status_string(0) == "ok"
+    assert "workspace" in N.status_string(N.M16_ERR_WORKSPACE)
+    assert lib.m16_abi_version() >= 1
+
+
+def test_workspace_bytes_grows_with_volume(lib):
+    from miccai2016_gb300 import _native as N
+    p = N.CutParams(0.2, 0.11, 1e-4, 100, 10, (ctypes.c_double * 3)(1, 1, 1))
+    small = lib.m16_maxflow_workspace_bytes(8, 8, 8, ctypes.byref(p))
+    big = lib.m16_maxflow_workspace_bytes(64, 64, 64, ctypes.byref(p))
+    assert 0 < small < big
+    assert big >= 64 ** 3 * 4 * 9
+    assert lib.m16_maxflow_workspace_bytes(0, 8, 8, ctypes.byref(p)) == 0
+
+
+def test_solve_rejects_bad_arguments_before_touching_the_gpu(lib):
+    from miccai2016_gb300 import _native as N
+    p = N.CutParams(0.2, 0.11, 1e-4, 100, 10, (ctypes.c_double * 3)(1, 1, 1))
+    it = ctypes.c_int32(0)
+    sq = (ctypes.c_double * 3)(1, 1, 1)
+    fake = ctypes.c_void_p(256)
+    # zero-sized volume
+    st = lib.m16_maxflow_solve(fake, fake, sq, None, None, 0.1, fake, fake, None, 0, 4, 4, ctypes.byref(p), fake,
+                               ctypes.byref(it), None, 0, None, fake, 1 << 20, None)
+    assert st == N.M16_ERR_BAD_SHAPE
+    # update < 1
+    p.update = 0
+    st = lib.m16_maxflow_solve(fake, fake, sq, None, None, 0.1, fake, fake, None, 4, 4, 4, ctypes.byref(p), fake,
+                               ctypes.byref(it), None, 0, None, fake, 1 << 20, None)
+    assert st == N.M16_ERR_BAD_ARG
+    p.update = 10
+    # workspace too small
+    st = lib.m16_maxflow_solve(fake, fake, sq, None, None, 0.1, fake, fake, None, 4, 4, 4, ctypes.byref(p), fake,
+                               ctypes.byref(it), None, 0, None, fake, 16, None)
+    assert st == N.M16_ERR_WORKSPACE
+    # neither constant nor per-voxel eigenvalues
+    st = lib.m16_maxflow_solve(fake, fake, None, None, None, 0.1, fake, fake, None, 4, 4, 4, ctypes.byref(p), fake,
+                               ctypes.byref(it), None, 0, None, fake, 1 << 20, None)
+    assert st == N.M16_ERR_BAD_ARG
