@@ -105,6 +105,38 @@ int m16_maxflow_solve_ex(const float *img, const float *quat3, const double *sqe
                          int32_t *n_residuals, void *workspace, size_t workspace_bytes, void *stream,
                          m16_solve_stats *stats);
 
+/* ---- gradient vector flow --------------------------------------------------
+ * Workspace bytes of m16_gvf_run; has_response says whether a response field
+ * will be passed, mags_cap bounds the convergence log (maxiter / update + 1). */
+size_t m16_gvf_workspace_bytes(int32_t d0, int32_t d1, int32_t d2, int32_t has_response, int32_t mags_cap);
+
+/*
+ * Explicit GVF iterations g <- g - dt * (r (g - v) - mu * lap(g)), replacing
+ * GvfGpu(vfield, params, voxel_size, response).execute()
+ * (src/processing/gradient_vector_flow.py:68-253) and its kernels gvfDelta,
+ * gvfUpdate, magDelta, gvfNormalize and response (src/clcode/gvf.cl:44-253).
+ *
+ *   v3           N x 3  the vector field (z, y, x, 3), the `vfield` argument
+ *   response     N      fidelity weight, or NULL for |v|^2 (the `response` argument)
+ *   voxel_size   host, 3 doubles [mm/voxel]
+ *   mu, dt       GvfParameters.mu and time_step_for(voxel_size, mu, 3)
+ *   first_iter   0 starts a new flow (g = 0); k > 0 continues one whose first k
+ *                iterations ran in earlier calls with the same workspace
+ *   n_iters      iterations to run in this call (GvfParameters.maxiter in one call)
+ *   update, tol  every iteration i with i % update == 0 computes mean|delta| and
+ *                stops the flow when it is below tol (tol = 0 never stops)
+ *   normalize    1 normalises the returned vectors to unit length (GvfParameters.normalize)
+ *   g3           N x 3  output: the current field
+ *   iterations, stopped, mags, n_mags   host outputs (all optional): iterations run in
+ *                total, whether tol stopped the flow, and the mean|delta| log
+ * Synchronizes `stream` before returning.
+ */
+int m16_gvf_run(const float *v3, const float *response, int32_t d0, int32_t d1, int32_t d2,
+                const double *voxel_size, double mu, double dt, int32_t first_iter, int32_t n_iters,
+                int32_t update, double tol, int32_t normalize, float *g3, int32_t *iterations,
+                int32_t *stopped, double *mags, int32_t mags_cap, int32_t *n_mags, void *workspace,
+                size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,6 +68,12 @@ def _declare(L):
                                     ctypes.POINTER(_i32), _vp, _sz, _vp]
     L.m16_maxflow_solve_ex.restype = ctypes.c_int
     L.m16_maxflow_solve_ex.argtypes = L.m16_maxflow_solve.argtypes + [ctypes.POINTER(SolveStats)]
+    L.m16_gvf_workspace_bytes.restype = _sz
+    L.m16_gvf_workspace_bytes.argtypes = [_i32, _i32, _i32, _i32, _i32]
+    L.m16_gvf_run.restype = ctypes.c_int
+    L.m16_gvf_run.argtypes = [_vp, _vp, _i32, _i32, _i32, _vp, _f64, _f64, _i32, _i32, _i32, _f64, _i32, _vp,
+                              ctypes.POINTER(_i32), ctypes.POINTER(_i32), _vp, _i32, ctypes.POINTER(_i32), _vp,
+                              _sz, _vp]
 
 
 def lib(build_if_missing: bool = True):

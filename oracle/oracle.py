@@ -75,6 +75,11 @@ def _declare_oracle(L):
     L.oracle_mf_update_u.argtypes = [_i64, _i64, _i64, _vp, ctypes.c_double, ctypes.c_double] + [_vp] * 9
     L.oracle_mf_update_tmp.restype = None
     L.oracle_mf_update_tmp.argtypes = [_i64, _vp, ctypes.c_double, _vp, _vp]
+    L.oracle_gvf_time_step.restype = ctypes.c_double
+    L.oracle_gvf_time_step.argtypes = [_vp, ctypes.c_double, ctypes.c_int]
+    L.oracle_gvf_run.restype = ctypes.c_int
+    L.oracle_gvf_run.argtypes = [_vp, _vp, _i64, _i64, _i64, _vp, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_double, ctypes.c_int, _vp, _vp, _vp]
 
 
 # ----------------------------------------------------------------------------
@@ -214,3 +219,69 @@ def ref_maxflow_solve(img, quats, eigs, alpha, cs, ct, labels=None, scaling=None
                 return u, it + 1, np.array(resid)
         kt(ctypes.c_long(n), _ptr(k), _ptr(tmp), _ptr(u))
     return u, num_iter, np.array(resid)
+
+
+# ----------------------------------------------------------------------------
+# gradient vector flow
+# ----------------------------------------------------------------------------
+
+def gvf_time_step(voxel_size, mu):
+    vs = np.asarray(np.multiply(voxel_size, np.ones(3)), dtype=np.float64)
+    return float(lib().oracle_gvf_time_step(_ptr(vs), mu, 3))
+
+
+def gvf_run(vfield, mu, maxiter, update, tol=0.0, normalize=False, voxel_size=None, response=None):
+    """GvfGpu(vfield, params, voxel_size, response).execute() on the CPU.
+    Returns (gvf (z,y,x,3) float32, iterations, mean-|delta| log)."""
+    v = _f32(vfield)
+    assert v.ndim == 4 and v.shape[-1] == 3
+    shape = v.shape[:3]
+    vs = np.asarray(np.ones(3) if voxel_size is None else np.multiply(voxel_size, np.ones(3)), np.float64)
+    r = None if response is None else _f32(response)
+    g = np.empty_like(v)
+    mags = np.zeros(maxiter // max(update, 1) + 2, np.float64)
+    nm = ctypes.c_int(0)
+    it = lib().oracle_gvf_run(_ptr(v), _ptr(r), shape[0], shape[1], shape[2], _ptr(vs), mu, maxiter, update,
+                              tol, int(bool(normalize)), _ptr(g), _ptr(mags), ctypes.byref(nm))
+    return g, int(it), mags[:nm.value].copy()
+
+
+def ref_gvf_run(vfield, mu, maxiter, update, tol=0.0, normalize=False, voxel_size=None, response=None):
+    """The reference's GVF loop (gradient_vector_flow.py:179-232) driving the
+    reference's own gvf.cl kernels through the shim."""
+    R = ref()
+    v = _f32(vfield)
+    shape = v.shape[:3]
+    n = int(np.prod(shape))
+    vs = np.asarray(np.ones(3) if voxel_size is None else np.multiply(voxel_size, np.ones(3)), np.float64)
+    dt = np.minimum(0.99, (np.min(vs) ** 3) / (2.01 ** 3 * mu))
+    rss = 1. / (vs ** 2)
+    k = np.array([mu, dt, rss[0], rss[1], rss[2]], np.float64)
+    vc = [np.ascontiguousarray(v[..., c]) for c in range(3)]
+    r = np.empty(shape, np.float32)
+    if response is None:
+        R.ref_gvf_response(ctypes.c_long(n), _ptr(r), _ptr(vc[0]), _ptr(vc[1]), _ptr(vc[2]))
+    else:
+        r[...] = response
+    g = [np.zeros(shape, np.float32) for _ in range(3)]
+    e = [np.zeros(shape, np.float32) for _ in range(3)]
+    mags = []
+    it = 0
+    for it in range(int(maxiter)):
+        R.ref_gvf_delta(shape[0], shape[1], shape[2], _ptr(k), _ptr(e[0]), _ptr(e[1]), _ptr(e[2]), _ptr(g[0]),
+                        _ptr(g[1]), _ptr(g[2]), _ptr(vc[0]), _ptr(vc[1]), _ptr(vc[2]), _ptr(r))
+        R.ref_gvf_update(ctypes.c_long(n), _ptr(k), _ptr(g[0]), _ptr(g[1]), _ptr(g[2]), _ptr(e[0]), _ptr(e[1]),
+                         _ptr(e[2]))
+        if not it % update:
+            m = np.empty(shape, np.float32)
+            R.ref_gvf_mag_delta(ctypes.c_long(n), _ptr(m), _ptr(e[0]), _ptr(e[1]), _ptr(e[2]))
+            mag = sum_abs(m) / n
+            mags.append(mag)
+            if mag < tol:
+                it += 1
+                break
+    else:
+        it = int(maxiter)
+    if normalize:
+        R.ref_gvf_normalize(ctypes.c_long(n), _ptr(g[0]), _ptr(g[1]), _ptr(g[2]))
+    return np.stack(g, axis=-1), it, np.array(mags)

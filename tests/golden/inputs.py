@@ -53,3 +53,34 @@ def maxflow_case(name):
 
 
 MAXFLOW_CASES = ("mf_const_unsup", "mf_point_sup", "mf_stop")
+
+
+def gvf_case(name):
+    """(vfield, kwargs) of one GVF fixture."""
+    if name == "gvf_basic":
+        rng = np.random.RandomState(21)
+        shape = (12, 10, 14)
+        kw = dict(mu=0.2, maxiter=40, update=7, tol=0.0, normalize=False, voxel_size=None)
+    elif name == "gvf_aniso_norm":
+        rng = np.random.RandomState(22)
+        shape = (9, 13, 6)
+        kw = dict(mu=10 ** 0.5, maxiter=30, update=10, tol=0.0, normalize=True, voxel_size=(1.5, 0.8, 1.1))
+    elif name == "gvf_tol":
+        rng = np.random.RandomState(23)
+        shape = (10, 10, 10)
+        kw = dict(mu=0.2, maxiter=200, update=5, tol=2e-3, normalize=False, voxel_size=None)
+    else:
+        raise KeyError(name)
+    return unit_field(rng, shape), kw
+
+
+def unit_field(rng, shape):
+    """Random directions scaled by uniform [0, 1) magnitudes, like the
+    vesselness-weighted direction fields GVF diffuses (|v| <= 1 keeps the
+    explicit scheme stable)."""
+    d = rng.normal(size=shape + (3,))
+    d /= np.maximum(np.linalg.norm(d, axis=-1, keepdims=True), 1e-12)
+    return (d * rng.uniform(0, 1, shape)[..., None]).astype(np.float32)
+
+
+GVF_CASES = ("gvf_basic", "gvf_aniso_norm", "gvf_tol")

@@ -30,7 +30,20 @@ def make_maxflow():
         print(name, u.shape, iters, len(resid), os.path.getsize(path))
 
 
+def make_gvf():
+    for name in I.GVF_CASES:
+        v, kw = I.gvf_case(name)
+        g, iters, mags = O.ref_gvf_run(v, **kw)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, g=g, iterations=np.int64(iters), mags=np.asarray(mags, np.float64))
+        print(name, g.shape, iters, len(mags), os.path.getsize(path))
+
+
 if __name__ == "__main__":
     if O.ref() is None:
         raise SystemExit("the reference checkout is needed to generate fixtures")
-    make_maxflow()
+    which = sys.argv[1:] or ["maxflow", "gvf"]
+    if "maxflow" in which:
+        make_maxflow()
+    if "gvf" in which:
+        make_gvf()
