@@ -75,6 +75,20 @@ def _declare_oracle(L):
     L.oracle_mf_update_u.argtypes = [_i64, _i64, _i64, _vp, ctypes.c_double, ctypes.c_double] + [_vp] * 9
     L.oracle_mf_update_tmp.restype = None
     L.oracle_mf_update_tmp.argtypes = [_i64, _vp, ctypes.c_double, _vp, _vp]
+    L.oracle_convolve.restype = None
+    L.oracle_convolve.argtypes = [ctypes.c_int, _i64, _i64, _i64, _vp, _vp, _vp, ctypes.c_int]
+    L.oracle_hessian.restype = None
+    L.oracle_hessian.argtypes = [_i64, _i64, _i64, _vp, _vp, _vp, _vp]
+    L.oracle_eigs.restype = None
+    L.oracle_eigs.argtypes = [_i64, _vp, _vp]
+    L.oracle_max_norm.restype = ctypes.c_float
+    L.oracle_max_norm.argtypes = [_i64, _vp]
+    L.oracle_update_vesselness.restype = None
+    L.oracle_update_vesselness.argtypes = [_i64, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                           ctypes.c_int]
+    L.oracle_frangi.restype = None
+    L.oracle_frangi.argtypes = [_i64, _i64, _i64, _vp, ctypes.c_int, _vp, _vp, ctypes.c_float, ctypes.c_float,
+                                ctypes.c_float, ctypes.c_int, _vp, _vp, _vp]
     L.oracle_gvf_time_step.restype = ctypes.c_double
     L.oracle_gvf_time_step.argtypes = [_vp, ctypes.c_double, ctypes.c_int]
     L.oracle_gvf_run.restype = ctypes.c_int
@@ -285,3 +299,137 @@ def ref_gvf_run(vfield, mu, maxiter, update, tol=0.0, normalize=False, voxel_siz
     if normalize:
         R.ref_gvf_normalize(ctypes.c_long(n), _ptr(g[0]), _ptr(g[1]), _ptr(g[2]))
     return np.stack(g, axis=-1), it, np.array(mags)
+
+
+# ----------------------------------------------------------------------------
+# Frangi vesselness
+# ----------------------------------------------------------------------------
+
+def gauss_taps(sigma, order, scaling_factor=1.0, n_sigmas=4, round_up=False):
+    """GaussianFilter3D._gauss_kernel_with (qfrangi_gpu.py:158-185), float32."""
+    sigma_sq = sigma ** 2
+
+    def gaussian(x):
+        result = np.exp(-.5 * x ** 2 / sigma_sq)
+        return result / np.sum(result)
+
+    orders = [lambda x: gaussian(x),
+              lambda x: gaussian(x) * (-x) / (sigma_sq),
+              lambda x: gaussian(x) * (x ** 2 - sigma_sq) / (sigma_sq ** 2),
+              lambda x: gaussian(x) * x * (3 * sigma_sq - x ** 2) / (sigma_sq ** 3)]
+    x_max = int(np.ceil(n_sigmas * sigma)) if round_up else int(n_sigmas * sigma + 0.5)
+    x_s = np.arange(-x_max, x_max + 1)
+    return np.require(scaling_factor * orders[order](x_s), np.float32, ["C", "A"])
+
+
+def frangi_scales(scales, voxel_size):
+    """M x 3 per-axis sigmas in voxels (qfrangi_gpu.py:590-592)."""
+    scales_mm = np.linspace(*scales).reshape(-1, 1)
+    scaling = np.divide(1., voxel_size).reshape(1, -1)
+    return np.dot(scales_mm, scaling)
+
+
+def scale_taps(sigma3, gamma=1.0):
+    """taps[axis][order] (order 0..2; index 3 unused) and radii of one scale,
+    with the scale-space factor sigma ** (order * gamma) (qfrangi_gpu.py:136-142)."""
+    taps = []
+    radius = []
+    for a in range(3):
+        s = float(sigma3[a])
+        row = [gauss_taps(s, o, s ** (o * gamma)) for o in range(3)]
+        row.append(row[0])
+        taps.append(row)
+        radius.append(len(row[0]) // 2)
+    return taps, radius
+
+
+def _tap_ptr_array(taps_list):
+    arrs = [t for scale in taps_list for axis in scale for t in axis]
+    ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+    return ptrs, arrs
+
+
+def convolve(volume, axis, taps):
+    v = _f32(volume)
+    out = np.empty_like(v)
+    t = _f32(taps)
+    lib().oracle_convolve(axis, v.shape[0], v.shape[1], v.shape[2], _ptr(out), _ptr(v), _ptr(t), len(t) // 2)
+    return out
+
+
+def hessian(img, sigma3):
+    """N x 6 Hessian (00, 11, 22, 01, 02, 12) of one scale."""
+    img = _f32(img)
+    taps, radius = scale_taps(sigma3)
+    ptrs, keep = _tap_ptr_array([taps])
+    rad = np.asarray(radius, np.int32)
+    h = np.empty(img.shape + (6,), np.float32)
+    lib().oracle_hessian(img.shape[0], img.shape[1], img.shape[2], _ptr(img), ptrs, _ptr(rad), _ptr(h))
+    return h
+
+
+def eigs(h6):
+    """Jacobi eigendecomposition: [l1, l2, l3 (ascending |l|), squeezed quaternion]."""
+    h = _f32(h6)
+    out = np.empty_like(h)
+    lib().oracle_eigs(h.size // 6, _ptr(h), _ptr(out))
+    return out
+
+
+def frangi(img, scales, voxel_size=None, alpha=0.5, beta=0.5, c=None, bright=True):
+    """VesselnessCalculation/FeatureFilter on the CPU: (vesselness, squeezed
+    quaternions, c per scale).  `scales` is the (start, stop, number) triple
+    in mm of VesselnessCalculation.Parameters."""
+    img = _f32(img)
+    vs = np.ones(3) if voxel_size is None else np.multiply(voxel_size, np.ones(3))
+    sig = frangi_scales(scales, vs)
+    per = [scale_taps(s) for s in sig]
+    ptrs, keep = _tap_ptr_array([p[0] for p in per])
+    rad = np.asarray([p[1] for p in per], np.int32).ravel()
+    val = np.empty(img.shape, np.float32)
+    quat = np.empty(img.shape + (3,), np.float32)
+    cu = np.zeros(len(sig), np.float32)
+    lib().oracle_frangi(img.shape[0], img.shape[1], img.shape[2], _ptr(img), len(sig), ptrs, _ptr(rad), alpha,
+                        beta, -1.0 if c is None else float(c), int(bool(bright)), _ptr(val), _ptr(quat), _ptr(cu))
+    return val, quat, cu
+
+
+def ref_frangi(img, scales, voxel_size=None, alpha=0.5, beta=0.5, c=None, bright=True):
+    """The reference's scale loop (qfrangi_gpu.py:511-580, 208-271, 383-439)
+    over its own convolve_naive.cl, qeigs.cl and frangi.cl kernels."""
+    R = ref()
+    img = _f32(img)
+    shape = img.shape
+    n = img.size
+    d0, d1, d2 = shape
+    vs = np.ones(3) if voxel_size is None else np.multiply(voxel_size, np.ones(3))
+    val = np.full(shape, -np.inf, np.float32)
+    quat = np.zeros(shape + (3,), np.float32)
+    cus = []
+    for s in frangi_scales(scales, vs):
+        taps, radius = scale_taps(s)
+        h = np.empty((6, n), np.float32)
+        for i in range(3):
+            for j in range(i + 1):
+                order = [0, 0, 0]
+                order[i] = 1
+                order[j] += 1
+                a = img.copy()
+                b = np.empty_like(a)
+                for ax in range(3):
+                    t = taps[ax][order[ax]]
+                    R.ref_convolve(ax, d0, d1, d2, _ptr(b), _ptr(a), _ptr(t), radius[ax])
+                    a, b = b, a
+                h[i if i == j else 2 + i + j] = a.ravel()
+        e = np.require(h.T, np.float32, ["C", "A"])
+        R.ref_eigs(ctypes.c_long(n), _ptr(e), _ptr(e))
+        if c is None:
+            nrm = np.empty(n, np.float32)
+            R.ref_calculate_norm(ctypes.c_long(n), _ptr(nrm), _ptr(e))
+            cc = np.float32(0.5 * np.fmax.reduce(nrm))
+        else:
+            cc = np.float32(c)
+        cus.append(cc)
+        R.ref_update_vesselness(ctypes.c_long(n), _ptr(val), _ptr(quat), _ptr(e), ctypes.c_float(0.5 if alpha is None else alpha),
+                                ctypes.c_float(beta), ctypes.c_float(cc), int(bool(bright)))
+    return val, quat, np.array(cus, np.float32)

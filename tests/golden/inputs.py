@@ -84,3 +84,22 @@ def unit_field(rng, shape):
 
 
 GVF_CASES = ("gvf_basic", "gvf_aniso_norm", "gvf_tol")
+
+
+def frangi_case(name):
+    """(image, kwargs of oracle.frangi) of one Frangi fixture."""
+    if name == "frangi_bright":
+        rng = np.random.RandomState(31)
+        shape = (10, 12, 11)
+        kw = dict(scales=(1, 3, 3), voxel_size=None, alpha=0.5, beta=0.5, c=None, bright=True)
+    elif name == "frangi_dark_aniso":
+        rng = np.random.RandomState(32)
+        shape = (11, 9, 20)
+        kw = dict(scales=(1.0, 2.0, 2), voxel_size=(1.5, 1.0, 0.8), alpha=0.5, beta=0.5, c=0.25, bright=False)
+    else:
+        raise KeyError(name)
+    img = rng.normal(0.5, 0.5, shape).astype(np.float32)
+    return img, kw
+
+
+FRANGI_CASES = ("frangi_bright", "frangi_dark_aniso")

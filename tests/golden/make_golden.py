@@ -39,11 +39,29 @@ def make_gvf():
         print(name, g.shape, iters, len(mags), os.path.getsize(path))
 
 
+def make_frangi():
+    for name in I.FRANGI_CASES:
+        img, kw = I.frangi_case(name)
+        val, quat, c = O.ref_frangi(img, **kw)
+        sig = O.frangi_scales(kw["scales"], np.ones(3) if kw["voxel_size"] is None else kw["voxel_size"])
+        h = np.stack([O.hessian(img, s) for s in sig[:1]])
+        e = np.empty_like(h)
+        for k in range(len(h)):
+            ek = h[k].reshape(-1, 6).copy()
+            O.ref().ref_eigs(O.ctypes.c_long(ek.shape[0]), O._ptr(ek), O._ptr(ek))
+            e[k] = ek.reshape(h[k].shape)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, val=val, quat=quat, c=c, hessian=h, eigs=e)
+        print(name, val.shape, c, os.path.getsize(path))
+
+
 if __name__ == "__main__":
     if O.ref() is None:
         raise SystemExit("the reference checkout is needed to generate fixtures")
-    which = sys.argv[1:] or ["maxflow", "gvf"]
+    which = sys.argv[1:] or ["maxflow", "gvf", "frangi"]
     if "maxflow" in which:
         make_maxflow()
     if "gvf" in which:
         make_gvf()
+    if "frangi" in which:
+        make_frangi()
