@@ -32,6 +32,7 @@ extern "C" {
 #define M16_ERR_WORKSPACE 3     /* workspace NULL, misaligned or smaller than required */
 #define M16_ERR_CUDA 4          /* a CUDA runtime call failed */
 #define M16_ERR_TIMEOUT 5       /* a bounded device-side wait gave up */
+#define M16_ERR_TOO_LARGE 6     /* the request exceeds the fixed scratch of m16_maxflow_solve_static */
 
 /* Human-readable name of a status code (static string). */
 const char *m16_status_string(int status);
@@ -104,6 +105,35 @@ int m16_maxflow_solve_ex(const float *img, const float *quat3, const double *sqe
                          float *u, int32_t *iterations, double *residuals, int32_t residuals_cap,
                          int32_t *n_residuals, void *workspace, size_t workspace_bytes, void *stream,
                          m16_solve_stats *stats);
+
+/*
+ * m16_maxflow_solve for callers that cannot allocate device memory.
+ *
+ * No counterpart in the reference: it is an addition of this library.  Some
+ * callers have no way to obtain device memory -- a plugin whose host owns all
+ * device memory and gives it no allocator, a foreign-language binding that
+ * needs a fixed footprint known at load time, a service that must not
+ * allocate while serving.  This entry point takes inputs and outputs like
+ * m16_maxflow_solve but no workspace: its scratch is a fixed 11 MiB array
+ * inside the library that every GPU loading the library reserves until the
+ * process exits.  Nothing is allocated by the call (no cudaMalloc, no
+ * allocating library routine).
+ *
+ * Limits: at most 262,144 voxels (e.g. 64 x 64 x 64) and at most 4,096
+ * residual checks (num_iter / update + 2 <= 4096); larger requests return
+ * M16_ERR_TOO_LARGE before any GPU work.  The first call on a device looks
+ * the array's device address up (once per device, with that device current);
+ * make that first call before any stream capture.  All calls share the one
+ * array: calls that overlap on the GPU (other streams, other host threads)
+ * race and must be serialised by the caller.  The solve initialises every
+ * scratch word it reads, so one call's leftovers never reach the next.
+ */
+int m16_maxflow_solve_static(const float *img, const float *quat3, const double *sqevals3,
+                             const float *sqeigs, const float *alpha, float alpha_scalar,
+                             const float *cs, const float *ct, const uint8_t *labels,
+                             int32_t d0, int32_t d1, int32_t d2, const m16_cut_params *params,
+                             float *u, int32_t *iterations, double *residuals, int32_t residuals_cap,
+                             int32_t *n_residuals, void *stream);
 
 /* ---- gradient vector flow --------------------------------------------------
  * Workspace bytes of m16_gvf_run; has_response says whether a response field

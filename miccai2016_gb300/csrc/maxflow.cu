@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -462,4 +463,80 @@ extern "C" int m16_maxflow_solve_ex(const float *img, const float *quat3, const 
         }
     }
     return M16_OK;
+}
+
+// ---- fixed-footprint variant: no allocation by anyone --------------------------
+//
+// m16_maxflow_solve takes its scratch from a workspace the caller allocates.
+// Some callers cannot allocate device memory at all: a plugin whose host owns
+// every byte of device memory through its own pool and hands it no allocator,
+// a language binding (Go, Java, ...) that wants a fixed device footprint known
+// at load time, or a service that must not allocate once it is serving.  For
+// them m16_maxflow_solve_static runs the same solve with its scratch in the
+// file-scope array below, which the CUDA module reserves on every device that
+// loads this library and which stays reserved until the process exits.
+//
+// Limits: at most kStaticMaxVoxels voxels (e.g. 64 x 64 x 64) and at most
+// kStaticMaxChecks residual checks (num_iter / update + 2 <= kStaticMaxChecks).
+
+namespace m16 {
+namespace {
+constexpr int64_t kStaticMaxVoxels = 262144;
+constexpr int kStaticMaxChecks = 4096;
+// hp0, hp1, hp2, pt, tmp (4 B each) + q4 (16 B) + block partials (<= 4 B per voxel,
+// every block covers at least one voxel) + max partials + control + residual log,
+// each region rounded up to 256 B
+constexpr size_t kStaticBytes = 11u << 20;   // 11 MiB >= 10,521,344 B needed at the limits
+
+std::mutex g_static_mu;
+void *g_static_scratch[64] = {};
+}  // namespace
+}  // namespace m16
+
+static __device__ __align__(256) unsigned char m16_static_scratch[m16::kStaticBytes];
+
+namespace m16 {
+namespace {
+// Device address of the scratch array on the current device.  The first call
+// on a device resolves it with cudaGetSymbolAddress (host code cannot use the
+// array's name as a device address) and caches it per device.
+int static_scratch_on_current_device(void **out)
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return M16_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_scratch[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, m16_static_scratch) != cudaSuccess || !p) return M16_ERR_CUDA;
+        g_static_scratch[dev] = p;
+    }
+    *out = g_static_scratch[dev];
+    return M16_OK;
+}
+}  // namespace
+}  // namespace m16
+
+extern "C" int m16_maxflow_solve_static(const float *img, const float *quat3, const double *sqevals3,
+                                        const float *sqeigs, const float *alpha, float alpha_scalar,
+                                        const float *cs, const float *ct, const uint8_t *labels,
+                                        int32_t d0, int32_t d1, int32_t d2, const m16_cut_params *params,
+                                        float *u, int32_t *iterations, double *residuals, int32_t residuals_cap,
+                                        int32_t *n_residuals, void *stream)
+{
+    // size checks first: nothing touches the GPU for a request that cannot fit
+    if (d0 < 1 || d1 < 1 || d2 < 1 || !params) return d0 < 1 || d1 < 1 || d2 < 1 ? M16_ERR_BAD_SHAPE : M16_ERR_BAD_ARG;
+    if (params->update < 1 || params->num_iter < 0) return M16_ERR_BAD_ARG;
+    if ((int64_t)d0 * d1 * d2 > kStaticMaxVoxels) return M16_ERR_TOO_LARGE;
+    if (params->num_iter / params->update + 2 > kStaticMaxChecks) return M16_ERR_TOO_LARGE;
+    const MfLayout L = mf_layout(d0, d1, d2, params->num_iter, params->update);
+    if (L.total > kStaticBytes) return M16_ERR_TOO_LARGE;
+    void *scratch = nullptr;
+    const int st = static_scratch_on_current_device(&scratch);
+    if (st != M16_OK) return st;
+    // The solve's initialisation kernels write every scratch word before it is
+    // read (flow state, control word, partial sums), so nothing of the previous
+    // call's contents leaks into this one.
+    return m16_maxflow_solve_ex(img, quat3, sqevals3, sqeigs, alpha, alpha_scalar, cs, ct, labels, d0, d1, d2,
+                                params, u, iterations, residuals, residuals_cap, n_residuals, scratch, kStaticBytes,
+                                stream, nullptr);
 }
