@@ -114,9 +114,21 @@ __global__ void mf_init_kernel(MfArgs a, const float *__restrict__ img, const fl
 }
 
 // ---- P: flow update and projection (update_qp.cl:150-232) -----------------
+//
+// Each thread walks its z-column in batches of kZB slices: all loads of a
+// batch are issued before any arithmetic, so every thread keeps ~10 kZB
+// independent loads in flight (the sweeps are memory-latency bound otherwise).
+
+#ifndef M16_MF_ZB
+#define M16_MF_ZB 2
+#endif
+#ifndef M16_MF_MINB
+#define M16_MF_MINB 1
+#endif
+constexpr int kZB = M16_MF_ZB;
 
 template <bool POINTWISE, bool ALPHA_ARR>
-__global__ void __launch_bounds__(kBX * kBY) mf_update_p_kernel(MfArgs a)
+__global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_p_kernel(MfArgs a)
 {
     if (__ldcg(&a.ctrl->stopped)) return;
     const int x = blockIdx.x * kBX + threadIdx.x;
@@ -128,40 +140,66 @@ __global__ void __launch_bounds__(kBX * kBY) mf_update_p_kernel(MfArgs a)
     int64_t i = ((int64_t)z0 * a.d1 + y) * a.d2 + x;
     const bool yin = y < a.d1 - 1, xin = x < a.d2 - 1;
     float t = __ldg(a.tmp + i);
-    for (int z = z0; z < z1; ++z, i += s0) {
-        const bool zin = z < a.d0 - 1;
-        const float tz = zin ? __ldg(a.tmp + i + s0) : 0.f;
-        const float ty = yin ? __ldg(a.tmp + i + a.d2) : 0.f;
-        const float tx = xin ? __ldg(a.tmp + i + 1) : 0.f;
-        const float3 g = make_float3(zin ? (tz - t) * a.ss0 : 0.f, yin ? (ty - t) * a.ss1 : 0.f,
-                                     xin ? (tx - t) * a.ss2 : 0.f);
-        const Rot R = quat2rot(__ldg(a.q4 + i));
-        float s0v = a.sq0, s1v = a.sq1, s2v = a.sq2, i0v = a.isq0, i1v = a.isq1, i2v = a.isq2;
-        if (POINTWISE) {
-            s0v = __ldg(a.sqeigs + 3 * i);
-            s1v = __ldg(a.sqeigs + 3 * i + 1);
-            s2v = __ldg(a.sqeigs + 3 * i + 2);
-            i0v = 1.f / s0v; i1v = 1.f / s1v; i2v = 1.f / s2v;
+    for (int zb = z0; zb < z1; zb += kZB, i += kZB * s0) {
+        float tz[kZB], ty[kZB], tx[kZB], al[kZB], h0[kZB], h1[kZB], h2[kZB];
+        float4 q[kZB];
+        float se0[kZB], se1[kZB], se2[kZB];
+#pragma unroll
+        for (int k = 0; k < kZB; ++k) {
+            if (zb + k < z1) {
+                const int64_t j = i + k * s0;
+                tz[k] = (zb + k < a.d0 - 1) ? __ldg(a.tmp + j + s0) : 0.f;
+                ty[k] = yin ? __ldg(a.tmp + j + a.d2) : 0.f;
+                tx[k] = xin ? __ldg(a.tmp + j + 1) : 0.f;
+                q[k] = __ldg(a.q4 + j);
+                al[k] = ALPHA_ARR ? __ldg(a.alpha + j) : a.alpha_scalar;
+                h0[k] = a.hp0[j];
+                h1[k] = a.hp1[j];
+                h2[k] = a.hp2[j];
+                if (POINTWISE) {
+                    se0[k] = __ldg(a.sqeigs + 3 * j);
+                    se1[k] = __ldg(a.sqeigs + 3 * j + 1);
+                    se2[k] = __ldg(a.sqeigs + 3 * j + 2);
+                }
+            }
         }
-        const float3 rg = rot_t(R, g);
-        const float3 rh = rot_t(R, make_float3(a.hp0[i], a.hp1[i], a.hp2[i]));
-        float3 p = make_float3(rh.x * i0v + rg.x * s0v, rh.y * i1v + rg.y * s1v, rh.z * i2v + rg.z * s2v);
-        const float nrm = sqrtf(p.x * p.x + p.y * p.y + p.z * p.z);
-        const float rad = ALPHA_ARR ? __ldg(a.alpha + i) : a.alpha_scalar;
-        const float sc = nrm > rad ? rad / nrm : 1.f;
-        p = make_float3(p.x * sc * s0v, p.y * sc * s1v, p.z * sc * s2v);
-        const float3 h = rot(R, p);
-        a.hp0[i] = h.x;
-        a.hp1[i] = h.y;
-        a.hp2[i] = h.z;
-        t = tz;
+#pragma unroll
+        for (int k = 0; k < kZB; ++k) {
+            if (zb + k < z1) {
+                const int64_t j = i + k * s0;
+                const float tc = k == 0 ? t : tz[k - 1];
+                const bool zin = zb + k < a.d0 - 1;
+                const float3 g = make_float3(zin ? (tz[k] - tc) * a.ss0 : 0.f, yin ? (ty[k] - tc) * a.ss1 : 0.f,
+                                             xin ? (tx[k] - tc) * a.ss2 : 0.f);
+                const Rot R = quat2rot(q[k]);
+                float s0v = a.sq0, s1v = a.sq1, s2v = a.sq2, i0v = a.isq0, i1v = a.isq1, i2v = a.isq2;
+                if (POINTWISE) {
+                    s0v = se0[k]; s1v = se1[k]; s2v = se2[k];
+                    i0v = 1.f / s0v; i1v = 1.f / s1v; i2v = 1.f / s2v;
+                }
+                // p = H^-1 hp + H^T (steps grad tmp) with H = R diag(sqrt eig)
+                const float3 rg = rot_t(R, g);
+                const float3 rh = rot_t(R, make_float3(h0[k], h1[k], h2[k]));
+                float3 p = make_float3(rh.x * i0v + rg.x * s0v, rh.y * i1v + rg.y * s1v,
+                                       rh.z * i2v + rg.z * s2v);
+                // project onto |p| <= alpha, then hp = H p
+                const float nrm = sqrtf(p.x * p.x + p.y * p.y + p.z * p.z);
+                const float sc = nrm > al[k] ? al[k] / nrm : 1.f;
+                p = make_float3(p.x * sc * s0v, p.y * sc * s1v, p.z * sc * s2v);
+                const float3 h = rot(R, p);
+                a.hp0[j] = h.x;
+                a.hp1[j] = h.y;
+                a.hp2[j] = h.z;
+            }
+        }
+        t = tz[kZB - 1];
     }
 }
 
 // ---- U: divergence, terminal flows, labels (update_qp.cl:241-300, 311-316) -
 
 template <bool SUPERVISED, bool CHECK>
-__global__ void __launch_bounds__(kBX * kBY) mf_update_u_kernel(MfArgs a)
+__global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_u_kernel(MfArgs a)
 {
     __shared__ float red[32];
     if (__ldcg(&a.ctrl->stopped)) return;
@@ -175,38 +213,55 @@ __global__ void __launch_bounds__(kBX * kBY) mf_update_u_kernel(MfArgs a)
         int64_t i = ((int64_t)z0 * a.d1 + y) * a.d2 + x;
         const bool ylo = y > 0, xlo = x > 0, yhi = y < a.d1 - 1, xhi = x < a.d2 - 1;
         float h0m = z0 > 0 ? __ldg(a.hp0 + i - s0) : 0.f;
-        for (int z = z0; z < z1; ++z, i += s0) {
-            const float h0 = __ldg(a.hp0 + i);
-            const float h1 = __ldg(a.hp1 + i);
-            const float h2 = __ldg(a.hp2 + i);
-            const float h1m = ylo ? __ldg(a.hp1 + i - a.d2) : 0.f;
-            const float h2m = xlo ? __ldg(a.hp2 + i - 1) : 0.f;
-            const float a0 = (z < a.d0 - 1 ? h0 : 0.f) - (z > 0 ? h0m : 0.f);
-            const float a1 = (yhi ? h1 : 0.f) - h1m;
-            const float a2 = (xhi ? h2 : 0.f) - h2m;
-            const float div = a0 * a.rs0 + a1 * a.rs1 + a2 * a.rs2;
-            const float uo = a.u[i];
-            // p_s = min(div + p_t - (u - s_off)/cc, C_s); p_t = min(-div + p_s + (u - t_off)/cc, C_t)
-            // with (s_off, t_off) = (1, 0) unsupervised and (!(l & 2), l & 1) with seeds l
-            float s_off = 1.f, t_off = 0.f;
-            if (SUPERVISED) {
-                const uint8_t l = __ldg(a.labels + i);
-                s_off = (float)(!(l & 2));
-                t_off = (float)(l & 1);
+        for (int zb = z0; zb < z1; zb += kZB, i += kZB * s0) {
+            float h0[kZB], h1[kZB], h2[kZB], h1m[kZB], h2m[kZB], uo[kZB], ptv[kZB], csv[kZB], ctv[kZB];
+            uint8_t lab[kZB];
+#pragma unroll
+            for (int k = 0; k < kZB; ++k) {
+                if (zb + k < z1) {
+                    const int64_t j = i + k * s0;
+                    h0[k] = __ldg(a.hp0 + j);
+                    h1[k] = __ldg(a.hp1 + j);
+                    h2[k] = __ldg(a.hp2 + j);
+                    h1m[k] = ylo ? __ldg(a.hp1 + j - a.d2) : 0.f;
+                    h2m[k] = xlo ? __ldg(a.hp2 + j - 1) : 0.f;
+                    uo[k] = a.u[j];
+                    ptv[k] = a.pt[j];
+                    csv[k] = __ldg(a.cs + j);
+                    ctv[k] = __ldg(a.ct + j);
+                    if (SUPERVISED) lab[k] = __ldg(a.labels + j);
+                }
             }
-            const float psx = div + a.pt[i] - a.rcc * (uo - s_off);
-            const float csv = __ldg(a.cs + i);
-            const float ps = csv < psx ? csv : psx;
-            const float ptx = -div + ps + a.rcc * (uo - t_off);
-            const float ctv = __ldg(a.ct + i);
-            const float ptn = ctv < ptx ? ctv : ptx;
-            const float err = div - ps + ptn;
-            const float un = uo - err / a.rcc;
-            a.pt[i] = ptn;
-            a.u[i] = un;
-            a.tmp[i] = err - un * a.rcc;
-            if (CHECK) acc += fabsf(err);
-            h0m = h0;
+#pragma unroll
+            for (int k = 0; k < kZB; ++k) {
+                if (zb + k < z1) {
+                    const int64_t j = i + k * s0;
+                    const int z = zb + k;
+                    const float prev0 = k == 0 ? h0m : h0[k - 1];
+                    const float a0 = (z < a.d0 - 1 ? h0[k] : 0.f) - (z > 0 ? prev0 : 0.f);
+                    const float a1 = (yhi ? h1[k] : 0.f) - h1m[k];
+                    const float a2 = (xhi ? h2[k] : 0.f) - h2m[k];
+                    const float div = a0 * a.rs0 + a1 * a.rs1 + a2 * a.rs2;
+                    // p_s = min(div + p_t - (u - s_off)/cc, C_s); p_t = min(-div + p_s + (u - t_off)/cc, C_t)
+                    // with (s_off, t_off) = (1, 0) unsupervised and (!(l & 2), l & 1) with seeds l
+                    float s_off = 1.f, t_off = 0.f;
+                    if (SUPERVISED) {
+                        s_off = (float)(!(lab[k] & 2));
+                        t_off = (float)(lab[k] & 1);
+                    }
+                    const float psx = div + ptv[k] - a.rcc * (uo[k] - s_off);
+                    const float ps = csv[k] < psx ? csv[k] : psx;
+                    const float ptx = -div + ps + a.rcc * (uo[k] - t_off);
+                    const float ptn = ctv[k] < ptx ? ctv[k] : ptx;
+                    const float err = div - ps + ptn;
+                    const float un = uo[k] - err / a.rcc;
+                    a.pt[j] = ptn;
+                    a.u[j] = un;
+                    a.tmp[j] = err - un * a.rcc;
+                    if (CHECK) acc += fabsf(err);
+                }
+            }
+            h0m = h0[kZB - 1];
         }
     }
     if (CHECK) {
@@ -251,12 +306,15 @@ struct MfLayout {
 
 constexpr int kMaxBlocks = 4 * kSMs;
 
+// z-slices per thread: enough blocks for 8 per SM, at most 16, a multiple of
+// the load batch once it reaches it
 inline int choose_zc(int d0, int d1, int d2)
 {
     const int64_t cols = div_up(d2, kBX) * div_up(d1, kBY);
     int64_t zc = (int64_t)d0 * cols / (8 * kSMs);
     if (zc < 1) zc = 1;
     if (zc > 16) zc = 16;
+    if (zc >= kZB) zc = zc / kZB * kZB;
     return (int)zc;
 }
 
