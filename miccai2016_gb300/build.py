@@ -15,8 +15,11 @@ from concurrent.futures import ThreadPoolExecutor
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
-OUT_DIR = os.path.join(PKG_DIR, "_lib")
+# M16_LIB_DIR builds/loads a tuning variant elsewhere; M16_NVCC_DEFINES adds
+# -D flags (e.g. "-DM16_MF_ZB=4") to every translation unit of that variant.
+OUT_DIR = os.environ.get("M16_LIB_DIR") or os.path.join(PKG_DIR, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
+EXTRA_DEFINES = os.environ.get("M16_NVCC_DEFINES", "").split()
 LIB_NAME = "libmiccai2016_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
@@ -53,7 +56,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if (not force and os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src)
                 and os.path.getmtime(obj) >= newest_hdr):
             return obj, False
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+        cmd = [nvcc] + ARCH + NVCC_FLAGS + EXTRA_DEFINES + ["-c", src, "-o", obj]
         proc = subprocess.run(cmd, capture_output=True, text=True)
         if proc.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, proc.stdout, proc.stderr))
