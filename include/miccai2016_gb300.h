@@ -34,6 +34,9 @@ extern "C" {
 #define M16_ERR_TIMEOUT 5       /* a bounded device-side wait gave up */
 #define M16_ERR_TOO_LARGE 6     /* the request exceeds the fixed scratch of m16_maxflow_solve_static */
 
+/* Longest Gaussian derivative kernel (taps = 2 * radius + 1) the Frangi entry points take. */
+#define M16_MAX_TAPS 127
+
 /* Human-readable name of a status code (static string). */
 const char *m16_status_string(int status);
 
@@ -166,6 +169,48 @@ int m16_gvf_run(const float *v3, const float *response, int32_t d0, int32_t d1, 
                 int32_t update, double tol, int32_t normalize, float *g3, int32_t *iterations,
                 int32_t *stopped, double *mags, int32_t mags_cap, int32_t *n_mags, void *workspace,
                 size_t workspace_bytes, void *stream);
+
+/* ---- Frangi vesselness -------------------------------------------------------
+ * Taps layout (host float32): for scale s, axis a (0 = z, 1 = y, 2 = x) and
+ * derivative order o in {0, 1, 2}, the 2*radius[s][a]+1 taps of the Gaussian
+ * derivative kernel, already multiplied by sigma**o, start at
+ * taps[((s * 3 + a) * 3 + o) * M16_MAX_TAPS].  They are the kernels of
+ * GaussianFilter3D._gauss_kernel_with (src/processing/qfrangi_gpu.py:158-185).
+ * radius (host int32) is nscales x 3.                                        */
+size_t m16_frangi_workspace_bytes(int32_t d0, int32_t d1, int32_t d2, int32_t nscales);
+
+/*
+ * Multi-scale Frangi vesselness, replacing VesselnessCalculation.execute /
+ * FeatureFilter.execute_for (src/processing/qfrangi_gpu.py:511-580, 696-753)
+ * with GaussianFilter3D + Hessian (:30-271, convolve_naive.cl), Eigendecomposition
+ * (qeigs.cl, eigenvalues ascending by absolute value) and VesselnessUpdate
+ * (frangi.cl, max.cl).
+ *   img      N        image (float32)
+ *   alpha, beta       Frangi weights (VesselnessCalculation.Parameters.alpha/.beta)
+ *   c        >= 0: the structureness weight; < 0: half the maximum Hessian norm
+ *            of each scale, as the reference does for c = None
+ *   bright   1 bright tubes on dark background, 0 dark on bright
+ *   val      N        output: maximum vesselness over the scales (-inf where no
+ *                     scale gave a number)
+ *   quat3    N x 3    output: squeezed quaternion of the eigenvectors (columns) at
+ *                     the maximising scale (0 where no scale gave a number)
+ *   c_used   host, nscales floats, optional: the c of every scale
+ */
+int m16_frangi(const float *img, int32_t d0, int32_t d1, int32_t d2, int32_t nscales, const float *taps,
+               const int32_t *radius, float alpha, float beta, float c, int32_t bright, float *val,
+               float *quat3, float *c_used, void *workspace, size_t workspace_bytes, void *stream);
+
+/* One scale's Hessian (N x 6: 00, 11, 22, 01, 02, 12), replacing
+ * Hessian.execute (qfrangi_gpu.py:208-271); taps/radius of one scale as above;
+ * workspace of m16_frangi_workspace_bytes(d0, d1, d2, 1). */
+int m16_hessian(const float *img, int32_t d0, int32_t d1, int32_t d2, const float *taps,
+                const int32_t *radius, float *h6, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Jacobi eigendecomposition of n symmetric 3x3 matrices (N x 6 in the order
+ * above) into [l1, l2, l3 ascending by |l|, squeezed quaternion], replacing
+ * Eigendecomposition.execute / eigs (qeigs.cl:146-256); NaN x 6 where 50
+ * sweeps do not converge.  h6 and out6 may be the same buffer. */
+int m16_eigs(const float *h6, int64_t n, float *out6, void *stream);
 
 #ifdef __cplusplus
 }

@@ -68,6 +68,15 @@ def _declare(L):
                                     ctypes.POINTER(_i32), _vp, _sz, _vp]
     L.m16_maxflow_solve_ex.restype = ctypes.c_int
     L.m16_maxflow_solve_ex.argtypes = L.m16_maxflow_solve.argtypes + [ctypes.POINTER(SolveStats)]
+    L.m16_frangi_workspace_bytes.restype = _sz
+    L.m16_frangi_workspace_bytes.argtypes = [_i32, _i32, _i32, _i32]
+    L.m16_frangi.restype = ctypes.c_int
+    L.m16_frangi.argtypes = [_vp, _i32, _i32, _i32, _i32, _vp, _vp, _f32, _f32, _f32, _i32, _vp, _vp, _vp, _vp,
+                             _sz, _vp]
+    L.m16_hessian.restype = ctypes.c_int
+    L.m16_hessian.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp]
+    L.m16_eigs.restype = ctypes.c_int
+    L.m16_eigs.argtypes = [_vp, _i64, _vp, _vp]
     L.m16_gvf_workspace_bytes.restype = _sz
     L.m16_gvf_workspace_bytes.argtypes = [_i32, _i32, _i32, _i32, _i32]
     L.m16_gvf_run.restype = ctypes.c_int

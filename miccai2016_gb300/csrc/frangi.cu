@@ -1,0 +1,528 @@
+// frangi.cu -- Frangi vesselness on GB300: Gaussian-derivative Hessian per
+// scale, 3x3 Jacobi eigendecomposition, vesselness and running maximum over
+// scales.  Replaces the reference's GaussianFilter3D/Hessian/Eigendecomposition/
+// VesselnessUpdate/VesselnessCalculation (src/processing/qfrangi_gpu.py:30-631)
+// and the kernels axis0/1/2 (src/clcode/convolve_naive.cl), eigs
+// (src/clcode/qeigs.cl), updateVesselness/calculateNorm (src/clcode/frangi.cl)
+// and redMax (src/clcode/max.cl).
+//
+// The six Hessian entries share their separable factors, so one scale costs
+// 15 one-dimensional passes instead of the reference's 18 (and no host round
+// trip): z-pass of orders 0/1/2 -> Z0, Z1, Z2; y-pass -> the six products
+//   A = y0 Z2 (-> 00), B = y2 Z0 (-> 11), C = y0 Z0 (-> 22),
+//   D = y1 Z1 (-> 01), E = y0 Z1 (-> 02), F = y1 Z0 (-> 12);
+// x-pass fused with the eigensolve: 00 = x0 A, 11 = x0 B, 22 = x2 C,
+// 01 = x0 D, 02 = x1 E, 12 = x1 F.  Every pass is a true convolution (taps
+// read reversed) with the reference's mirror boundary (period 2(n-1)).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <float.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace m16 {
+namespace {
+
+constexpr int kMaxTaps = M16_MAX_TAPS;   // 2 * radius + 1 <= kMaxTaps
+constexpr int kBX = 32, kBY = 8;
+
+// taps of one axis, orders 0, 1, 2 (already scaled by sigma ** order)
+struct AxisTaps {
+    float t[3][kMaxTaps];
+    int radius;
+};
+
+// mirror-completed index with period 2 (n - 1) (convolve_naive.cl:25-63)
+__device__ __forceinline__ int mirror(int p, int n)
+{
+    if (n == 1) return 0;
+    const int period = 2 * (n - 1);
+    p %= period;
+    if (p < 0) p += period;
+    return p < n ? p : period - p;
+}
+
+inline int fr_zc(int d0, int d1, int d2)
+{
+    const int64_t cols = div_up(d2, kBX) * div_up(d1, kBY);
+    int64_t zc = (int64_t)d0 * cols / (8 * kSMs);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(8, zc));
+}
+
+// ---- pass 1: z (axis 0), orders 0, 1, 2 ------------------------------------
+__global__ void __launch_bounds__(kBX * kBY) fr_conv_z_kernel(const float *__restrict__ img, float *__restrict__ z0,
+                                                              float *__restrict__ z1, float *__restrict__ z2, int d0,
+                                                              int d1, int d2, int zc, AxisTaps tp)
+{
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y * kBY + threadIdx.y;
+    if (x >= d2 || y >= d1) return;
+    const int za = blockIdx.z * zc, zb = min(za + zc, d0);
+    const int64_t s0 = (int64_t)d1 * d2;
+    const int64_t col = (int64_t)y * d2 + x;
+    const int r = tp.radius, K = 2 * r + 1;
+    for (int z = za; z < zb; ++z) {
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        const bool inner = z - r >= 0 && z + r < d0;
+        for (int j = 0; j < K; ++j) {
+            const int m = inner ? z - r + j : mirror(z - r + j, d0);
+            const float v = __ldg(img + col + m * s0);
+            const int k = K - 1 - j;
+            a0 = fmaf(tp.t[0][k], v, a0);
+            a1 = fmaf(tp.t[1][k], v, a1);
+            a2 = fmaf(tp.t[2][k], v, a2);
+        }
+        const int64_t i = col + z * s0;
+        z0[i] = a0;
+        z1[i] = a1;
+        z2[i] = a2;
+    }
+}
+
+// ---- pass 2: y (axis 1), the six products ----------------------------------
+__global__ void __launch_bounds__(kBX * kBY) fr_conv_y_kernel(const float *__restrict__ z0, const float *__restrict__ z1,
+                                                              const float *__restrict__ z2, float *__restrict__ six,
+                                                              int d0, int d1, int d2, int zc, AxisTaps tp)
+{
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y * kBY + threadIdx.y;
+    if (x >= d2 || y >= d1) return;
+    const int za = blockIdx.z * zc, zb = min(za + zc, d0);
+    const int64_t s0 = (int64_t)d1 * d2, n = s0 * d0;
+    const int r = tp.radius, K = 2 * r + 1;
+    const bool inner = y - r >= 0 && y + r < d1;
+    for (int z = za; z < zb; ++z) {
+        const int64_t plane = (int64_t)z * s0 + x;
+        float A = 0.f, B = 0.f, C = 0.f, D = 0.f, E = 0.f, F = 0.f;
+        for (int j = 0; j < K; ++j) {
+            const int m = inner ? y - r + j : mirror(y - r + j, d1);
+            const int64_t idx = plane + (int64_t)m * d2;
+            const float v0 = __ldg(z0 + idx), v1 = __ldg(z1 + idx), v2 = __ldg(z2 + idx);
+            const int k = K - 1 - j;
+            const float t0 = tp.t[0][k], t1 = tp.t[1][k], t2 = tp.t[2][k];
+            A = fmaf(t0, v2, A);
+            B = fmaf(t2, v0, B);
+            C = fmaf(t0, v0, C);
+            D = fmaf(t1, v1, D);
+            E = fmaf(t0, v1, E);
+            F = fmaf(t1, v0, F);
+        }
+        const int64_t i = plane + (int64_t)y * d2;
+        six[i] = A;
+        six[n + i] = B;
+        six[2 * n + i] = C;
+        six[3 * n + i] = D;
+        six[4 * n + i] = E;
+        six[5 * n + i] = F;
+    }
+}
+
+// ---- Jacobi eigensolve (qeigs.cl:35-256), eigenvalues ascending by |lambda| -
+
+__constant__ float kSorterQuat[6][4] = {{0.f, 0.f, 0.f, 1.f},
+                                        {0.f, -0.70710678118654752f, 0.70710678118654752f, 0.f},
+                                        {-0.70710678118654752f, 0.70710678118654752f, 0.f, 0.f},
+                                        {-0.5f, -0.5f, -0.5f, 0.5f},
+                                        {0.5f, 0.5f, 0.5f, 0.5f},
+                                        {-0.70710678118654752f, 0.f, 0.70710678118654752f, 0.f}};
+
+__device__ __forceinline__ bool eigcmp(float a, float b) { return fabsf(a) < fabsf(b); }
+
+// squeezed quaternion of q (scalar part last), qsqueezeLast (quaternion_math.h:45-69)
+__device__ __forceinline__ void squeeze_last(const float q[4], float v[3])
+{
+    const float q1 = q[0], q2 = q[1], q3 = q[2], q0 = q[3];
+    const float q1spq2s = q1 * q1 + q2 * q2;
+    const bool c1 = q1spq2s < FLT_EPSILON;
+    const bool c2 = c1 || (1.f - q1spq2s) < FLT_EPSILON;
+    const float q1q3 = q1 * q3, q2q0 = q2 * q0, q1q0 = q1 * q0, q2q3 = q2 * q3;
+    auto satan2 = [](float a, float b) { return (a == 0.f && b == 0.f) ? 0.f : atan2f(a, b); };
+    v[0] = satan2(q1q3 + q2q0, q1q0 - q2q3);
+    v[1] = c2 ? (c1 ? 0.f : 3.14159265358979323846f) : acosf(fminf(fmaxf(1.f - 2.f * q1spq2s, -1.f), 1.f));
+    float at2 = c2 ? (q1 * q2 - q0 * q3) : (q1q3 - q2q0);
+    at2 = satan2(at2, c2 ? (0.5f - (q2 * q2 + q3 * q3)) : (q1q0 + q2q3));
+    v[2] = c2 ? (-at2 + v[0] * (c1 ? -1.f : 1.f)) : at2;
+}
+
+__device__ __forceinline__ void eig3(const float h[6], float out[6])
+{
+    const float GAMMA = 5.8284271247461900976f, C_STAR = 0.9238795325112867561f, S_STAR = 0.3826834323650897717f;
+    float on[3] = {h[0], h[1], h[2]};
+    float off[3] = {h[5], h[4], h[3]};
+    float oq[4] = {0.f, 0.f, 0.f, 1.f};
+    const float tol = fmaxf(fmaxf(fmaxf(fabsf(on[0]), fabsf(on[1])), fmaxf(fabsf(on[2]), fabsf(off[0]))),
+                            fmaxf(fabsf(off[1]), fabsf(off[2]))) * FLT_EPSILON;
+    for (int it = 0; it < 50; ++it) {
+        if (fabsf(off[0]) + fabsf(off[1]) + fabsf(off[2]) <= tol) {
+            // sortEigs (qeigs.cl:60-92)
+            int o0, o1, o2, ot;
+            float vt;
+            bool c = eigcmp(on[0], on[1]);
+            vt = on[0]; on[0] = c ? on[0] : on[1]; o0 = c ? 0 : 1; on[1] = c ? on[1] : vt; o1 = c ? 1 : 0;
+            c = eigcmp(on[1], on[2]);
+            vt = on[1]; ot = o1; on[1] = c ? on[1] : on[2]; o1 = c ? o1 : 2; on[2] = c ? on[2] : vt; o2 = c ? 2 : ot;
+            c = eigcmp(on[0], on[1]);
+            vt = on[0]; ot = o0; on[0] = c ? on[0] : on[1]; o0 = c ? o0 : o1; on[1] = c ? on[1] : vt; o1 = c ? o1 : ot;
+            const int sk = (o0 << 1) | (o1 > o2 ? 1 : 0);
+            const float l0 = kSorterQuat[sk][0], l1 = kSorterQuat[sk][1], l2 = kSorterQuat[sk][2],
+                        l3 = kSorterQuat[sk][3];
+            float q[4];
+            q[3] = l3 * oq[3] - (l0 * oq[0] + l1 * oq[1] + l2 * oq[2]);
+            q[0] = l3 * oq[0] + l0 * oq[3] + l1 * oq[2] - l2 * oq[1];
+            q[1] = l3 * oq[1] - l0 * oq[2] + l1 * oq[3] + l2 * oq[0];
+            q[2] = l3 * oq[2] + l0 * oq[1] - l1 * oq[0] + l2 * oq[3];
+            q[3] = -q[3];   // eigenvectors in columns
+            float sq[3];
+            squeeze_last(q, sq);
+            out[0] = on[0]; out[1] = on[1]; out[2] = on[2];
+            out[3] = sq[0]; out[4] = sq[1]; out[5] = sq[2];
+            return;
+        }
+#pragma unroll
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq < 2 ? 0 : 1;
+            const int q = pq == 0 ? 1 : 2;
+            const int r = 3 ^ (p | q);
+            // approximate Givens rotation (McAdams et al.)
+            float c = 2.f * (on[q] - on[p]);
+            float s = off[r];
+            float t1 = s * s, t2 = c * c;
+            const bool cond = GAMMA * t1 < t2;
+            t1 = rsqrtf(t1 + t2);
+            c = cond ? t1 * c : C_STAR;
+            s = cond ? t1 * s : S_STAR;
+            // accumulate the quaternion (scalar part last)
+            t1 = c * oq[p] - s * oq[q];
+            t2 = c * oq[q] + s * oq[p];
+            oq[p] = t1; oq[q] = t2;
+            const float sr = (r == 1) ? s : -s;
+            t1 = c * oq[3] + sr * oq[r];
+            t2 = c * oq[r] - sr * oq[3];
+            oq[3] = t1; oq[r] = t2;
+            // rotate the matrix
+            t1 = 1.f - 2.f * s * s;
+            s = 2.f * c * s;
+            c = t1;
+            t1 = off[r] * c + on[p] * s;
+            t2 = on[q] * c + off[r] * s;
+            on[p] = c * (on[p] * c - off[r] * s) - s * (off[r] * c - on[q] * s);
+            on[q] = c * t2 + s * t1;
+            off[r] = c * t1 - s * t2;
+            t2 = off[q];
+            off[q] = c * t2 - s * off[p];
+            off[p] = c * off[p] + s * t2;
+        }
+    }
+    for (int k = 0; k < 6; ++k) out[k] = NAN;
+}
+
+// Frangi response of one eigen-triple (frangi.cl:46-92)
+__device__ __forceinline__ float vesselness(const float e[6], float alpha, float beta, float c, bool bright)
+{
+    const float l1 = fabsf(e[0]);
+    float l2 = bright ? e[1] : -e[1];
+    float l3 = bright ? e[2] : -e[2];
+    const bool valid = l2 < 0.f && l3 < 0.f;
+    l2 = fabsf(l2);
+    l3 = fabsf(l3);
+    const float rb = l1 / (sqrtf(l2 * l3) + FLT_MIN);
+    const float ra = l2 / (l3 + FLT_MIN);
+    const float ss = l1 * l1 + l2 * l2 + l3 * l3;
+    const float ta = ra / alpha, tb = rb / beta;
+    return (valid ? 1.f : 0.f) * ((1.f - expf(-0.5f * ta * ta)) * expf(-0.5f * tb * tb) *
+                                  (1.f - expf(-0.5f * ss / (c * c))));
+}
+
+struct FrArgs {
+    int d0, d1, d2, zc;
+    float alpha, beta, c;   // c < 0: read the per-scale c from *c_dev
+    int bright;
+    const float *six;
+    float *eig6;            // N x 6, or null when the update is fused
+    float *val, *quat3;
+    float *partials;        // per-block max Hessian norm
+    const float *c_dev;
+};
+
+// ---- pass 3: x (axis 2) fused with the eigensolve ----------------------------
+template <bool FUSED_UPDATE>
+__global__ void __launch_bounds__(kBX * kBY) fr_conv_x_eig_kernel(FrArgs a, AxisTaps tp)
+{
+    __shared__ float red[32];
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y * kBY + threadIdx.y;
+    float mx = -INFINITY;
+    if (x < a.d2 && y < a.d1) {
+        const int za = blockIdx.z * a.zc, zb = min(za + a.zc, a.d0);
+        const int64_t s0 = (int64_t)a.d1 * a.d2, n = s0 * a.d0;
+        const int r = tp.radius, K = 2 * r + 1;
+        const bool inner = x - r >= 0 && x + r < a.d2;
+        for (int z = za; z < zb; ++z) {
+            const int64_t row = (int64_t)z * s0 + (int64_t)y * a.d2;
+            float h[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int j = 0; j < K; ++j) {
+                const int m = inner ? x - r + j : mirror(x - r + j, a.d2);
+                const int64_t idx = row + m;
+                const int k = K - 1 - j;
+                const float t0 = tp.t[0][k], t1 = tp.t[1][k], t2 = tp.t[2][k];
+                h[0] = fmaf(t0, __ldg(a.six + idx), h[0]);
+                h[1] = fmaf(t0, __ldg(a.six + n + idx), h[1]);
+                h[2] = fmaf(t2, __ldg(a.six + 2 * n + idx), h[2]);
+                h[3] = fmaf(t0, __ldg(a.six + 3 * n + idx), h[3]);
+                h[4] = fmaf(t1, __ldg(a.six + 4 * n + idx), h[4]);
+                h[5] = fmaf(t1, __ldg(a.six + 5 * n + idx), h[5]);
+            }
+            float e[6];
+            eig3(h, e);
+            const int64_t i = row + x;
+            if (FUSED_UPDATE) {
+                const float v = vesselness(e, a.alpha, a.beta, a.c, a.bright != 0);
+                if (v > a.val[i]) {
+                    a.val[i] = v;
+                    a.quat3[3 * i] = e[3];
+                    a.quat3[3 * i + 1] = e[4];
+                    a.quat3[3 * i + 2] = e[5];
+                }
+            } else {
+                float2 *o = reinterpret_cast<float2 *>(a.eig6 + 6 * i);
+                o[0] = make_float2(e[0], e[1]);
+                o[1] = make_float2(e[2], e[3]);
+                o[2] = make_float2(e[4], e[5]);
+                // calculateNorm + redMax (NaN-neutral)
+                mx = fmaxf(mx, sqrtf(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]));
+            }
+        }
+    }
+    if (!FUSED_UPDATE) {
+        // block maximum (fmaxf ignores NaN as the reference's fmax does)
+        const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        if ((tid & 31) == 0) red[tid >> 5] = mx;
+        __syncthreads();
+        if (tid == 0) {
+            float m = red[0];
+            for (int w = 1; w < (kBX * kBY) / 32; ++w) m = fmaxf(m, red[w]);
+            a.partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = m;
+        }
+    }
+}
+
+// c = 0.5 * max norm of one scale (qfrangi_gpu.py:429-433)
+__global__ void fr_c_kernel(const float *__restrict__ part, int nparts, float *c_out)
+{
+    __shared__ float s[256];
+    float m = -INFINITY;
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) m = fmaxf(m, part[k]);
+    s[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = blockDim.x >> 1; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] = fmaxf(s[threadIdx.x], s[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *c_out = 0.5f * (s[0] == -INFINITY ? NAN : s[0]);
+}
+
+// updateVesselness (frangi.cl:46-92) from the stored eigendecompositions
+__global__ void fr_update_kernel(FrArgs a, int64_t n)
+{
+    const float c = *a.c_dev;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 *p = reinterpret_cast<const float2 *>(a.eig6 + 6 * i);
+        const float2 e01 = p[0], e23 = p[1], e45 = p[2];
+        const float e[6] = {e01.x, e01.y, e23.x, e23.y, e45.x, e45.y};
+        const float v = vesselness(e, a.alpha, a.beta, c, a.bright != 0);
+        if (v > a.val[i]) {
+            a.val[i] = v;
+            a.quat3[3 * i] = e[3];
+            a.quat3[3 * i + 1] = e[4];
+            a.quat3[3 * i + 2] = e[5];
+        }
+    }
+}
+
+__global__ void fr_init_kernel(float *val, float *quat3, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        val[i] = -INFINITY;
+        quat3[3 * i] = 0.f;
+        quat3[3 * i + 1] = 0.f;
+        quat3[3 * i + 2] = 0.f;
+    }
+}
+
+__global__ void fr_eigs_kernel(const float *__restrict__ in6, float *__restrict__ out6, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float h[6], e[6];
+        for (int k = 0; k < 6; ++k) h[k] = in6[6 * i + k];
+        eig3(h, e);
+        for (int k = 0; k < 6; ++k) out6[6 * i + k] = e[k];
+    }
+}
+
+// interleave the x-pass of the six products into an N x 6 Hessian (tests)
+__global__ void fr_conv_x_hessian_kernel(const float *__restrict__ six, float *__restrict__ h6, int d0, int d1, int d2,
+                                         int zc, AxisTaps tp)
+{
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y * kBY + threadIdx.y;
+    if (x >= d2 || y >= d1) return;
+    const int za = blockIdx.z * zc, zb = min(za + zc, d0);
+    const int64_t s0 = (int64_t)d1 * d2, n = s0 * d0;
+    const int r = tp.radius, K = 2 * r + 1;
+    for (int z = za; z < zb; ++z) {
+        const int64_t row = (int64_t)z * s0 + (int64_t)y * d2;
+        float h[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int j = 0; j < K; ++j) {
+            const int64_t idx = row + mirror(x - r + j, d2);
+            const int k = K - 1 - j;
+            h[0] = fmaf(tp.t[0][k], __ldg(six + idx), h[0]);
+            h[1] = fmaf(tp.t[0][k], __ldg(six + n + idx), h[1]);
+            h[2] = fmaf(tp.t[2][k], __ldg(six + 2 * n + idx), h[2]);
+            h[3] = fmaf(tp.t[0][k], __ldg(six + 3 * n + idx), h[3]);
+            h[4] = fmaf(tp.t[1][k], __ldg(six + 4 * n + idx), h[4]);
+            h[5] = fmaf(tp.t[1][k], __ldg(six + 5 * n + idx), h[5]);
+        }
+        for (int k = 0; k < 6; ++k) h6[6 * (row + x) + k] = h[k];
+    }
+}
+
+struct FrLayout {
+    size_t z, six, eig, part, cdev, total;
+    int nparts;
+};
+
+inline FrLayout fr_layout(int d0, int d1, int d2, int nscales)
+{
+    FrLayout L;
+    const int64_t n = (int64_t)d0 * d1 * d2;
+    const int zc = fr_zc(d0, d1, d2);
+    L.nparts = (int)(div_up(d2, kBX) * div_up(d1, kBY) * div_up(d0, zc));
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
+    L.z = take(3 * n * 4);
+    L.six = take(6 * n * 4);
+    L.eig = take(6 * n * 4);
+    L.part = take((size_t)L.nparts * 4);
+    L.cdev = take((size_t)std::max(nscales, 1) * 4);
+    L.total = off;
+    return L;
+}
+
+bool fill_taps(AxisTaps &tp, const float *taps_axis, int radius)
+{
+    if (radius < 0 || 2 * radius + 1 > kMaxTaps) return false;
+    tp.radius = radius;
+    for (int o = 0; o < 3; ++o)
+        for (int k = 0; k < kMaxTaps; ++k) tp.t[o][k] = k < 2 * radius + 1 ? taps_axis[o * kMaxTaps + k] : 0.f;
+    return true;
+}
+
+int hessian_passes(const float *img, int d0, int d1, int d2, const float *taps, const int *radius, char *ws,
+                   const FrLayout &L, cudaStream_t st, AxisTaps *tpx)
+{
+    AxisTaps tpz, tpy;
+    if (!fill_taps(tpz, taps, radius[0]) || !fill_taps(tpy, taps + 3 * kMaxTaps, radius[1]) ||
+        !fill_taps(*tpx, taps + 6 * kMaxTaps, radius[2]))
+        return M16_ERR_BAD_ARG;
+    const int64_t n = (int64_t)d0 * d1 * d2;
+    const int zc = fr_zc(d0, d1, d2);
+    const dim3 block(kBX, kBY, 1);
+    const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)div_up(d0, zc));
+    float *z = (float *)(ws + L.z);
+    fr_conv_z_kernel<<<grid, block, 0, st>>>(img, z, z + n, z + 2 * n, d0, d1, d2, zc, tpz);
+    fr_conv_y_kernel<<<grid, block, 0, st>>>(z, z + n, z + 2 * n, (float *)(ws + L.six), d0, d1, d2, zc, tpy);
+    M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}
+
+}  // namespace
+}  // namespace m16
+
+using namespace m16;
+
+extern "C" size_t m16_frangi_workspace_bytes(int32_t d0, int32_t d1, int32_t d2, int32_t nscales)
+{
+    if (d0 < 1 || d1 < 1 || d2 < 1) return 0;
+    return fr_layout(d0, d1, d2, nscales).total;
+}
+
+extern "C" int m16_frangi(const float *img, int32_t d0, int32_t d1, int32_t d2, int32_t nscales, const float *taps,
+                          const int32_t *radius, float alpha, float beta, float c, int32_t bright, float *val,
+                          float *quat3, float *c_used, void *workspace, size_t workspace_bytes, void *stream)
+{
+    if (d0 < 1 || d1 < 1 || d2 < 1 || (int64_t)d0 * d1 * d2 > ((int64_t)1 << 33)) return M16_ERR_BAD_SHAPE;
+    if (!img || !taps || !radius || !val || !quat3 || nscales < 1) return M16_ERR_BAD_ARG;
+    const FrLayout L = fr_layout(d0, d1, d2, nscales);
+    if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *ws = (char *)workspace;
+    const int64_t n = (int64_t)d0 * d1 * d2;
+    const int blocks1d = (int)std::min<int64_t>(8 * kSMs, div_up(n, 256));
+    fr_init_kernel<<<blocks1d, 256, 0, st>>>(val, quat3, n);
+    FrArgs a;
+    a.d0 = d0; a.d1 = d1; a.d2 = d2; a.zc = fr_zc(d0, d1, d2);
+    a.alpha = alpha; a.beta = beta; a.c = c; a.bright = bright;
+    a.six = (const float *)(ws + L.six);
+    a.eig6 = (float *)(ws + L.eig);
+    a.val = val; a.quat3 = quat3;
+    a.partials = (float *)(ws + L.part);
+    float *cdev = (float *)(ws + L.cdev);
+    const dim3 block(kBX, kBY, 1);
+    const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)div_up(d0, a.zc));
+    for (int s = 0; s < nscales; ++s) {
+        AxisTaps tpx;
+        const int rc = hessian_passes(img, d0, d1, d2, taps + (size_t)s * 9 * kMaxTaps, radius + 3 * s, ws, L, st, &tpx);
+        if (rc != M16_OK) return rc;
+        if (c >= 0.f) {
+            fr_conv_x_eig_kernel<true><<<grid, block, 0, st>>>(a, tpx);
+        } else {
+            a.c_dev = cdev + s;
+            fr_conv_x_eig_kernel<false><<<grid, block, 0, st>>>(a, tpx);
+            fr_c_kernel<<<1, 256, 0, st>>>(a.partials, L.nparts, cdev + s);
+            fr_update_kernel<<<blocks1d, 256, 0, st>>>(a, n);
+        }
+        M16_CUDA_TRY(cudaGetLastError());
+    }
+    if (c_used) {
+        if (c >= 0.f) {
+            for (int s = 0; s < nscales; ++s) c_used[s] = c;
+        } else {
+            M16_CUDA_TRY(cudaMemcpyAsync(c_used, cdev, (size_t)nscales * 4, cudaMemcpyDeviceToHost, st));
+            M16_CUDA_TRY(cudaStreamSynchronize(st));
+        }
+    }
+    return M16_OK;
+}
+
+extern "C" int m16_hessian(const float *img, int32_t d0, int32_t d1, int32_t d2, const float *taps,
+                           const int32_t *radius, float *h6, void *workspace, size_t workspace_bytes, void *stream)
+{
+    if (d0 < 1 || d1 < 1 || d2 < 1) return M16_ERR_BAD_SHAPE;
+    if (!img || !taps || !radius || !h6) return M16_ERR_BAD_ARG;
+    const FrLayout L = fr_layout(d0, d1, d2, 1);
+    if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    AxisTaps tpx;
+    const int rc = hessian_passes(img, d0, d1, d2, taps, radius, (char *)workspace, L, st, &tpx);
+    if (rc != M16_OK) return rc;
+    const int zc = fr_zc(d0, d1, d2);
+    const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)div_up(d0, zc));
+    fr_conv_x_hessian_kernel<<<grid, dim3(kBX, kBY, 1), 0, st>>>((const float *)((char *)workspace + L.six), h6, d0,
+                                                                 d1, d2, zc, tpx);
+    M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}
+
+extern "C" int m16_eigs(const float *h6, int64_t n, float *out6, void *stream)
+{
+    if (n < 0 || (n > 0 && (!h6 || !out6))) return M16_ERR_BAD_ARG;
+    if (n == 0) return M16_OK;
+    const int blocks = (int)std::min<int64_t>(8 * kSMs, div_up(n, 256));
+    fr_eigs_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(h6, out6, n);
+    M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}
