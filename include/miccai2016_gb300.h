@@ -212,6 +212,38 @@ int m16_hessian(const float *img, int32_t d0, int32_t d1, int32_t d2, const floa
  * sweeps do not converge.  h6 and out6 may be the same buffer. */
 int m16_eigs(const float *h6, int64_t n, float *out6, void *stream);
 
+/* ---- direction sign adjustment and transformation completion ------------------ */
+
+/* Ridge candidates of a vesselness response: 1 where resp > threshold and resp
+ * exceeds its 8 trilinearly sampled neighbours in the plane of the 2nd and 3rd
+ * eigenvectors (outside the volume counts -1), else 0.  Replaces RawRidgeDetector
+ * (src/processing/ridge_detection.py:12-77) and detectRidges (detect_ridges.cl:34-102).
+ * resp N, quat3 N x 3 squeezed quaternions, ridge N output.  d0 <= 65535. */
+int m16_detect_ridges(const float *resp, const float *quat3, int32_t d0, int32_t d1, int32_t d2,
+                      double threshold, float *ridge, void *stream);
+
+/* Main direction (first eigenvector column) of each squeezed quaternion,
+ * replacing extractMainDirections (adjust_directions.cl:29-43) as used by
+ * AdvancedAdjuster._qeigs_to_main_dirs (adjust_directions.py:341-362).
+ * quat3 and dirs3 (n x 3) may be the same buffer. */
+int m16_extract_main_directions(const float *quat3, int64_t n, float *dirs3, void *stream);
+
+/* Completion of each vector to a right-handed orthonormal frame, converted to a
+ * squeezed quaternion, replacing TransformationCompleter.complete
+ * (adjust_directions.py:486-504) / completeTransformations (adjust_directions.cl:68-100).
+ * dirs3 and quat3 (n x 3) may be the same buffer. */
+int m16_complete_transformations(const float *dirs3, int64_t n, float *quat3, void *stream);
+
+/* Sign of every direction flipped where its dot product with the direction of
+ * the nearest ridge point (squared distance scaled by `scaling3`, ties to the
+ * lowest index) is negative, in place.  Replaces
+ * AdvancedAdjuster._adjust_all_directions (adjust_directions.py:419-446) /
+ * adjustNonRidgeSigns (adjust_directions.cl:182-246); the ridge list is given
+ * as plain device arrays (coords num_ridge x 3 uint16 in axis order 0, 1, 2;
+ * rdirs num_ridge x 3 float32) instead of 8192-wide images.  scaling3 host. */
+int m16_adjust_nonridge_signs(float *dirs3, int32_t d0, int32_t d1, int32_t d2, const uint16_t *coords,
+                              const float *rdirs, int64_t num_ridge, const double *scaling3, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

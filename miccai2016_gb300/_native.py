@@ -77,6 +77,14 @@ def _declare(L):
     L.m16_hessian.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp]
     L.m16_eigs.restype = ctypes.c_int
     L.m16_eigs.argtypes = [_vp, _i64, _vp, _vp]
+    L.m16_detect_ridges.restype = ctypes.c_int
+    L.m16_detect_ridges.argtypes = [_vp, _vp, _i32, _i32, _i32, _f64, _vp, _vp]
+    L.m16_extract_main_directions.restype = ctypes.c_int
+    L.m16_extract_main_directions.argtypes = [_vp, _i64, _vp, _vp]
+    L.m16_complete_transformations.restype = ctypes.c_int
+    L.m16_complete_transformations.argtypes = [_vp, _i64, _vp, _vp]
+    L.m16_adjust_nonridge_signs.restype = ctypes.c_int
+    L.m16_adjust_nonridge_signs.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp, _i64, _vp, _vp]
     L.m16_gvf_workspace_bytes.restype = _sz
     L.m16_gvf_workspace_bytes.argtypes = [_i32, _i32, _i32, _i32, _i32]
     L.m16_gvf_run.restype = ctypes.c_int

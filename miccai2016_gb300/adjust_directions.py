@@ -1,0 +1,246 @@
+"""
+Neighbour-consistent sign adjustment of the vesselness main directions and
+their completion to full frames -- the drop-in for the reference module of the
+same name (src/processing/adjust_directions.py).
+
+AdvancedAdjuster keeps the reference's sequence (adjust_directions.py:213-256):
+ridge candidates on the GPU, hysteresis on the host, main directions on the
+GPU, the minimum spanning tree over the ridge points and the sign propagation
+along it on the host (ridge_mst.py: SciPy's Kruskal tree with a stable order
+of equal distances, without the reference's dense R x R matrix), ridge
+cleaning on the host, and the nearest-ridge sign flip of every voxel on the
+GPU (m16_adjust_nonridge_signs).  TransformationCompleter
+runs m16_complete_transformations.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+from scipy.ndimage import label
+
+from . import _native as N
+from .parameters import TreePrintable
+from .ridge_detection import RawRidgeDetector, hysteresis_threshold
+from .ridge_mst import propagate_signs, ridge_mst_edges
+
+
+class AdvancedAdjuster(TreePrintable):
+    """adjust_directions.py:25-446"""
+
+    def __init__(self, threshold, qeigs, response, voxel_size=1, ridge_detection_only=False, clean_ridge=True,
+                 loader=None):
+        self.__threshold = None
+        self.__qeigs = None
+        self.__response = None
+        self.__voxel_size = None
+        self.__ridge_detection_only = None
+        self.__clean_ridge = None
+        self.__ridge = None
+        self.__main_dirs_unadjusted = None
+        self._ridge_detector = None
+        self._hysteresis = None
+        self._dtype = np.float32
+        self._loader = loader  # accepted for compatibility, unused
+        if threshold is not None:
+            self.threshold = threshold
+        if qeigs is not None:
+            self.qeigs = qeigs
+        if response is not None:
+            self.response = response
+        if voxel_size is not None:
+            self.voxel_size = voxel_size
+        self.ridge_detection_only = ridge_detection_only
+        self.clean_ridge = clean_ridge
+
+    # -- properties (adjust_directions.py:105-186) -----------------------------
+    @property
+    def threshold(self):
+        return self.__threshold
+
+    @threshold.setter
+    def threshold(self, value):
+        try:
+            len(value)
+            value = tuple(sorted(value))
+            self._hysteresis = True
+            lower = value[0]
+        except TypeError:
+            self._hysteresis = False
+            lower = value
+        if value != self.__threshold:
+            self.__threshold = value
+            self._ridge_detector = RawRidgeDetector(self._loader, lower)
+
+    @property
+    def qeigs(self):
+        return self.__qeigs
+
+    @qeigs.setter
+    def qeigs(self, value):
+        self.__qeigs = np.require(value, dtype=self._dtype, requirements=["C", "A"])
+
+    @property
+    def response(self):
+        return self.__response
+
+    @response.setter
+    def response(self, value):
+        self.__response = np.require(value, dtype=self._dtype, requirements=["C", "A"])
+
+    @property
+    def voxel_size(self):
+        return self.__voxel_size
+
+    @voxel_size.setter
+    def voxel_size(self, value):
+        self.__voxel_size = tuple(np.multiply(np.ones(3), value))
+
+    @property
+    def ridge_detection_only(self):
+        return self.__ridge_detection_only
+
+    @ridge_detection_only.setter
+    def ridge_detection_only(self, value):
+        self.__ridge_detection_only = value
+
+    @property
+    def clean_ridge(self):
+        return self.__clean_ridge
+
+    @clean_ridge.setter
+    def clean_ridge(self, value):
+        self.__clean_ridge = value
+
+    @property
+    def ridge(self):
+        """After execute(): the detected (and possibly cleaned) ridge."""
+        return self.__ridge
+
+    @property
+    def main_dirs_unadjusted(self):
+        """After execute(): the extracted, not yet adjusted main directions."""
+        return self.__main_dirs_unadjusted
+
+    # -- the sequence (adjust_directions.py:213-256) ---------------------------
+    def execute(self, verbose=True):
+        """Returns the sign-adjusted main directions, (z, y, x, 3) float32, or
+        None when ridge_detection_only."""
+        assert self.response.shape == self.qeigs.shape[:3] and self.qeigs.shape[3] == 3
+        torch = N.torch_mod()
+        self._d_qeigs = N.to_device_f32(self.qeigs)
+        labeled_ridge = self._label_ridge()
+        adjusted = None
+        if (not self.ridge_detection_only) or self.clean_ridge:
+            main_dirs = self._qeigs_to_main_dirs()
+            ridge_coords, ridge_dirs = self._adjust_ridge_directions(labeled_ridge, main_dirs)
+            if self.clean_ridge:
+                labeled_ridge = self._do_clean_ridge(labeled_ridge, ridge_coords, ridge_dirs)
+                if not self.ridge_detection_only:
+                    ridge_coords, ridge_dirs = self._adjust_ridge_directions(labeled_ridge, main_dirs)
+            if not self.ridge_detection_only:
+                adjusted = self._adjust_all_directions(ridge_coords, ridge_dirs)
+        del self._d_qeigs
+        torch.cuda.current_stream().synchronize()
+        return adjusted
+
+    def _label_ridge(self):
+        """adjust_directions.py:258-288"""
+        ridge = self._ridge_detector.detect(self.response, self._d_qeigs)
+        ridge = np.require(ridge, np.float32, ["C", "A", "W"])
+        if self._hysteresis:
+            sure = np.logical_and(ridge, self.response >= self.threshold[1])
+            ridge[:] = hysteresis_threshold(ridge, sure)
+        self.__ridge = ridge
+        return ridge
+
+    def _do_clean_ridge(self, labeled_ridge, ridge_coords, ridge_dirs):
+        """Keep the ceil(3 ln(e + n)) 26-connected ridge segments whose summed
+        directions are longest (adjust_directions.py:290-339).  Per segment the
+        directions are summed in the reference's order (C order of the voxels)."""
+        scaled = ridge_dirs * self.__voxel_size   # float32 * tuple -> float64, as in the reference
+        components = label(labeled_ridge, structure=np.ones((3, 3, 3), dtype=int))[0]
+        labels = np.unique(components)[1:]
+        point_label = components[tuple(np.asarray(ridge_coords, np.intp).T)]
+        order = np.argsort(point_label, kind="stable")
+        sorted_labels = point_label[order]
+        starts = np.searchsorted(sorted_labels, labels, side="left")
+        ends = np.searchsorted(sorted_labels, labels, side="right")
+        lengths = {}
+        for lab, s, e in zip(labels, starts, ends):
+            lengths[lab] = np.linalg.norm(np.sum(scaled[order[s:e]], axis=0))
+        ordered = sorted(lengths, key=lambda k: lengths[k], reverse=True)
+        boundary = int(np.ceil(3 * np.log(np.e + len(ordered))))
+        print("Keeping %s of %s labels." % (boundary, len(ordered)))
+        kept = ordered[:boundary]
+        cleaned = np.isin(components, kept).astype(labeled_ridge.dtype).reshape(components.shape)
+        self.__ridge = cleaned
+        return cleaned
+
+    def _qeigs_to_main_dirs(self):
+        """adjust_directions.py:341-362: the device quaternion buffer is
+        overwritten with the main directions, which are also returned."""
+        n = self._d_qeigs.numel() // 3
+        st = N.lib().m16_extract_main_directions(N.ptr(self._d_qeigs), n, N.ptr(self._d_qeigs), N.stream_ptr())
+        N.check("m16_extract_main_directions", st)
+        main_dirs = self._d_qeigs.cpu().numpy()
+        self.__main_dirs_unadjusted = main_dirs.copy()
+        return main_dirs
+
+    def _adjust_ridge_directions(self, labeled_ridge, main_dirs):
+        """MST over the ridge points, sign propagation from point 0
+        (adjust_directions.py:365-417).  Returns (coords uint16 R x 3,
+        directions float32 R x 3).  The tree is SciPy's Kruskal tree with
+        equal distances taken in (i, j) order, computed without the dense
+        distance matrix (ridge_mst.py)."""
+        coords = np.argwhere(labeled_ridge)   # C order, as zip(*np.where(...))
+        if len(coords) == 0:
+            raise ValueError("no ridge points: nothing to propagate directions along")
+        a, b = ridge_mst_edges(coords, self.voxel_size)
+        dirs = main_dirs[coords[:, 0], coords[:, 1], coords[:, 2]]
+        adjusted = propagate_signs(len(coords), a, b, dirs)
+        return np.asarray(coords, dtype=np.uint16, order="C"), adjusted
+
+    def _adjust_all_directions(self, ridge_coords, ridge_dirs):
+        """Nearest-ridge sign flip of every voxel on the GPU
+        (adjust_directions.py:419-446)."""
+        torch = N.torch_mod()
+        assert len(ridge_coords) == len(ridge_dirs)
+        # uint16 coordinates travel as int16 (same bits; the kernel reads uint16)
+        coords = torch.from_numpy(np.ascontiguousarray(ridge_coords, dtype=np.uint16).view(np.int16)).to(N.device())
+        rdirs = N.to_device_f32(ridge_dirs)
+        d0, d1, d2 = self.response.shape
+        sc = (ctypes.c_double * 3)(*[float(v) for v in self.voxel_size])
+        st = N.lib().m16_adjust_nonridge_signs(N.ptr(self._d_qeigs), d0, d1, d2, N.ptr(coords), N.ptr(rdirs),
+                                              len(ridge_coords), sc, N.stream_ptr())
+        N.check("m16_adjust_nonridge_signs", st)
+        return self._d_qeigs.cpu().numpy()
+
+
+class TransformationCompleter(TreePrintable):
+    """adjust_directions.py:449-517: complete each vector to a right-handed
+    orthonormal frame and return its squeezed quaternion."""
+
+    def __init__(self, dirs, loader=None):
+        self.__dirs = None
+        self._dtype = np.float32
+        self._loader = loader  # accepted for compatibility, unused
+        if dirs is not None:
+            self.dirs = dirs
+
+    def complete(self):
+        torch = N.torch_mod()
+        on_device = N.is_torch(self.__dirs)
+        d = N.to_device_f32(self.__dirs)
+        out = torch.empty_like(d)
+        st = N.lib().m16_complete_transformations(N.ptr(d), d.numel() // 3, N.ptr(out), N.stream_ptr())
+        N.check("m16_complete_transformations", st)
+        return out if on_device else out.cpu().numpy()
+
+    @property
+    def dirs(self):
+        return self.__dirs
+
+    @dirs.setter
+    def dirs(self, value):
+        self.__dirs = value if N.is_torch(value) else np.require(value, dtype=self._dtype, requirements=["C", "A"])

@@ -1,0 +1,314 @@
+// directions.cu -- the direction kernels of the sign adjustment and the
+// transformation completion: detectRidges (src/clcode/detect_ridges.cl:34-102),
+// extractMainDirections, completeTransformations and adjustNonRidgeSigns
+// (src/clcode/adjust_directions.cl:29-246).
+//
+// These decide discrete outcomes (ridge or not, nearest ridge point, sign), so
+// their arithmetic follows the reference's rounding sequence: explicit _rn
+// intrinsics instead of contracted multiply-adds, and the quaternion
+// expansion's trigonometry in double rounded to float (the reference's
+// OpenCL C promotes `* 0.5` to double).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <float.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace m16 {
+namespace {
+
+constexpr int kBX = 32, kBY = 8;
+
+// qexpand with the reference's precision: half angles rounded to float, the
+// cosines and sines evaluated in double and rounded to float.
+__device__ __forceinline__ void qexpand_ref(float phi, float theta, float psi, float q[4])
+{
+    const float pp = __fmul_rn(__fadd_rn(phi, psi), 0.5f);
+    const float pm = __fmul_rn(__fsub_rn(phi, psi), 0.5f);
+    const float ct = (float)cos((double)theta * 0.5);
+    const float st = (float)sin((double)theta * 0.5);
+    const float cpp = (float)cos((double)pp), spp = (float)sin((double)pp);
+    const float cpm = (float)cos((double)pm), spm = (float)sin((double)pm);
+    q[0] = __fmul_rn(cpp, ct);
+    q[1] = __fmul_rn(cpm, st);
+    q[2] = __fmul_rn(spm, st);
+    q[3] = __fmul_rn(spp, ct);
+}
+
+__device__ __forceinline__ float sq_rn(float x) { return __fmul_rn(x, x); }
+
+// columns of quat2matFloat3 (quaternion_math.h:257-289), no contraction
+__device__ __forceinline__ void quat_cols(const float q[4], float c0[3], float c1[3], float c2[3])
+{
+    const float qx2 = sq_rn(q[1]), qy2 = sq_rn(q[2]), qz2 = sq_rn(q[3]);
+    const float qwqx = __fmul_rn(q[0], q[1]), qwqy = __fmul_rn(q[0], q[2]), qwqz = __fmul_rn(q[0], q[3]);
+    const float qxqy = __fmul_rn(q[1], q[2]), qxqz = __fmul_rn(q[1], q[3]), qyqz = __fmul_rn(q[2], q[3]);
+    if (c0) {
+        c0[0] = __fsub_rn(1.f, __fmul_rn(2.f, __fadd_rn(qy2, qz2)));
+        c0[1] = __fmul_rn(2.f, __fadd_rn(qxqy, qwqz));
+        c0[2] = __fmul_rn(2.f, __fsub_rn(qxqz, qwqy));
+    }
+    if (c1) {
+        c1[0] = __fmul_rn(2.f, __fsub_rn(qxqy, qwqz));
+        c1[1] = __fsub_rn(1.f, __fmul_rn(2.f, __fadd_rn(qx2, qz2)));
+        c1[2] = __fmul_rn(2.f, __fadd_rn(qyqz, qwqx));
+    }
+    if (c2) {
+        c2[0] = __fmul_rn(2.f, __fadd_rn(qxqz, qwqy));
+        c2[1] = __fmul_rn(2.f, __fsub_rn(qyqz, qwqx));
+        c2[2] = __fsub_rn(1.f, __fmul_rn(2.f, __fadd_rn(qx2, qy2)));
+    }
+}
+
+// ---- detectRidges -----------------------------------------------------------
+__global__ void __launch_bounds__(kBX * kBY) dr_detect_ridges_kernel(const float *__restrict__ resp,
+                                                                     const float *__restrict__ quat3,
+                                                                     float *__restrict__ ridge, int d0, int d1,
+                                                                     int d2, double threshold)
+{
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y * kBY + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= d2 || y >= d1) return;
+    const int64_t i = ((int64_t)z * d1 + y) * d2 + x;
+    float q[4], c1[3], c2[3];
+    qexpand_ref(quat3[3 * i], quat3[3 * i + 1], quat3[3 * i + 2], q);
+    quat_cols(q, nullptr, c1, c2);
+    const float pos[3] = {(float)z, (float)y, (float)x};
+    const int dims[3] = {d0, d1, d2};
+    float maxv = -INFINITY;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const float a = (float)((-1) * (j < 3) + (j > 4));
+        const float b = (float)((j % 3) - 1 + (j == 4));
+        float p[3];
+        int o[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            p[k] = __fadd_rn(__fadd_rn(pos[k], __fmul_rn(a, c1[k])), __fmul_rn(b, c2[k]));
+            o[k] = (int)p[k];   // toward zero, as convert_int3
+            p[k] = __fsub_rn(p[k], (float)o[k]);
+        }
+        float v = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int r0 = k >> 2, r1 = (k >> 1) & 1, r2 = k & 1;
+            const int a0 = o[0] + r0, a1 = o[1] + r1, a2 = o[2] + r2;
+            const float w0 = r0 ? p[0] : __fsub_rn(1.f, p[0]);
+            const float w1 = r1 ? p[1] : __fsub_rn(1.f, p[1]);
+            const float w2 = r2 ? p[2] : __fsub_rn(1.f, p[2]);
+            const bool out = a0 < 0 || a1 < 0 || a2 < 0 || a0 >= dims[0] || a1 >= dims[1] || a2 >= dims[2];
+            const float s = out ? -1.f : __ldg(resp + ((int64_t)a0 * d1 + a1) * d2 + a2);
+            v = __fadd_rn(v, __fmul_rn(__fmul_rn(__fmul_rn(s, w0), w1), w2));
+        }
+        maxv = v > maxv ? v : maxv;
+    }
+    const float r = resp[i];
+    ridge[i] = ((double)r > threshold && r > maxv) ? 1.f : 0.f;
+}
+
+// ---- extractMainDirections ----------------------------------------------------
+__global__ void dr_extract_kernel(const float *in3, float *out3, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float q[4], c0[3];
+        qexpand_ref(in3[3 * i], in3[3 * i + 1], in3[3 * i + 2], q);
+        quat_cols(q, c0, nullptr, nullptr);
+        out3[3 * i] = c0[0];
+        out3[3 * i + 1] = c0[1];
+        out3[3 * i + 2] = c0[2];
+    }
+}
+
+// ---- completeTransformations ----------------------------------------------------
+__device__ __forceinline__ void normalize3(const float v[3], float o[3])
+{
+    const float l2 = __fadd_rn(__fadd_rn(sq_rn(v[0]), sq_rn(v[1])), sq_rn(v[2]));
+    if (l2 == 0.f) { o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; return; }
+    const float l = __fsqrt_rn(l2);
+    o[0] = __fdiv_rn(v[0], l); o[1] = __fdiv_rn(v[1], l); o[2] = __fdiv_rn(v[2], l);
+}
+
+__device__ __forceinline__ float rsqrt_ref(float x) { return __fdiv_rn(1.f, __fsqrt_rn(x)); }
+
+// qsqueeze (quaternion_math.h:20-39), scalar part first, written literally
+// (products with the 0/1 conditions included: they decide the sign of zero
+// that atan2 sees)
+__device__ __forceinline__ void qsqueeze_ref(const float q[4], float v[3])
+{
+    const float q1spq2s = __fadd_rn(sq_rn(q[1]), sq_rn(q[2]));
+    const bool c1 = q1spq2s < FLT_EPSILON;
+    const bool c2 = c1 || __fsub_rn(1.f, q1spq2s) < FLT_EPSILON;
+    const float f2 = c2 ? 1.f : 0.f, nf2 = c2 ? 0.f : 1.f;
+    const float q1q3 = __fmul_rn(q[1], q[3]), q2q0 = __fmul_rn(q[2], q[0]);
+    const float q1q0 = __fmul_rn(q[1], q[0]), q2q3 = __fmul_rn(q[2], q[3]);
+    auto satan2 = [](double a, double b) {
+        return (a == 0.0 && b == 0.0) ? 0.f : atan2f((float)a, (float)b);
+    };
+    v[0] = satan2(__fadd_rn(q1q3, q2q0), __fsub_rn(q1q0, q2q3));
+    const float ac = acosf(fminf(fmaxf(__fsub_rn(1.f, __fmul_rn(2.f, q1spq2s)), -1.f), 1.f));
+    v[1] = (float)((c1 ? 0.0 : 3.14159265358979323846) * (double)f2 + (double)__fmul_rn(ac, nf2));
+    float at2 = __fadd_rn(__fmul_rn(__fsub_rn(__fmul_rn(q[1], q[2]), __fmul_rn(q[0], q[3])), f2),
+                          __fmul_rn(__fsub_rn(q1q3, q2q0), nf2));
+    const double den = (0.5 - (double)__fadd_rn(sq_rn(q[2]), sq_rn(q[3]))) * (double)f2 +
+                       (double)__fmul_rn(__fadd_rn(q1q0, q2q3), nf2);
+    at2 = satan2((double)at2, den);
+    v[2] = __fadd_rn(__fmul_rn(__fadd_rn(-at2, __fmul_rn(v[0], c1 ? -1.f : 1.f)), f2), __fmul_rn(at2, nf2));
+}
+
+__global__ void dr_complete_kernel(const float *in3, float *out3, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v[3] = {in3[3 * i], in3[3 * i + 1], in3[3 * i + 2]};
+        float e0[3], e1[3], e2[3], t[3];
+        normalize3(v, e0);
+        if (fabsf(e0[0]) > fabsf(e0[1])) { t[0] = -e0[2]; t[1] = 0.f; t[2] = e0[0]; }
+        else { t[0] = 0.f; t[1] = e0[2]; t[2] = -e0[1]; }
+        normalize3(t, e1);
+        e2[0] = __fsub_rn(__fmul_rn(e0[1], e1[2]), __fmul_rn(e0[2], e1[1]));
+        e2[1] = __fsub_rn(__fmul_rn(e0[2], e1[0]), __fmul_rn(e0[0], e1[2]));
+        e2[2] = __fsub_rn(__fmul_rn(e0[0], e1[1]), __fmul_rn(e0[1], e1[0]));
+        // mat2quat (quaternion_math.h:301-340), m[row][col] with columns e0, e1, e2
+        const float m00 = e0[0], m01 = e1[0], m02 = e2[0];
+        const float m10 = e0[1], m11 = e1[1], m12 = e2[1];
+        const float m20 = e0[2], m21 = e1[2], m22 = e2[2];
+        float q[4];
+        float s = __fadd_rn(__fadd_rn(m00, m11), m22);
+        if (s > 0.f) {
+            s = (float)((double)rsqrt_ref((float)((double)s + 1.0)) * 0.5);
+            q[0] = (float)(0.25 / (double)s);
+            q[1] = __fmul_rn(__fsub_rn(m21, m12), s);
+            q[2] = __fmul_rn(__fsub_rn(m02, m20), s);
+            q[3] = __fmul_rn(__fsub_rn(m10, m01), s);
+        } else if (m00 > m11 && m00 > m22) {
+            s = (float)((double)rsqrt_ref((float)(1.0 + (double)m00 - (double)m11 - (double)m22)) * 0.5);
+            q[0] = __fmul_rn(__fsub_rn(m21, m12), s);
+            q[1] = (float)(0.25 / (double)s);
+            q[2] = __fmul_rn(__fadd_rn(m01, m10), s);
+            q[3] = __fmul_rn(__fadd_rn(m02, m20), s);
+        } else if (m11 > m22) {
+            s = (float)((double)rsqrt_ref((float)(1.0 + (double)m11 - (double)m00 - (double)m22)) * 0.5);
+            q[0] = __fmul_rn(__fsub_rn(m02, m20), s);
+            q[1] = __fmul_rn(__fadd_rn(m01, m10), s);
+            q[2] = (float)(0.25 / (double)s);
+            q[3] = __fmul_rn(__fadd_rn(m12, m21), s);
+        } else {
+            s = (float)((double)rsqrt_ref((float)(1.0 + (double)m22 - (double)m00 - (double)m11)) * 0.5);
+            q[0] = __fmul_rn(__fsub_rn(m10, m01), s);
+            q[1] = __fmul_rn(__fadd_rn(m02, m20), s);
+            q[2] = __fmul_rn(__fadd_rn(m12, m21), s);
+            q[3] = (float)(0.25 / (double)s);
+        }
+        float sq[3];
+        qsqueeze_ref(q, sq);
+        out3[3 * i] = sq[0];
+        out3[3 * i + 1] = sq[1];
+        out3[3 * i + 2] = sq[2];
+    }
+}
+
+// ---- adjustNonRidgeSigns ----------------------------------------------------------
+// Brute-force nearest ridge point per voxel: ridge points are staged through
+// shared memory in tiles; every thread scans them in ascending index order with
+// a strict <, so the lowest index wins ties exactly as in the reference.
+constexpr int kTile = 1024;
+
+__global__ void __launch_bounds__(256) dr_adjust_kernel(float *__restrict__ dirs3, const uint16_t *__restrict__ coords,
+                                                        const float *__restrict__ rdirs, int64_t R, int d0, int d1,
+                                                        int d2, float s0, float s1, float s2)
+{
+    __shared__ float sc[3][kTile];
+    const int64_t n = (int64_t)d0 * d1 * d2;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool act = i < n;
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f;
+    if (act) {
+        p2 = (float)(i % d2);
+        p1 = (float)((i / d2) % d1);
+        p0 = (float)(i / ((int64_t)d1 * d2));
+    }
+    float best = INFINITY;
+    int64_t bj = 0;
+    for (int64_t t0 = 0; t0 < R; t0 += kTile) {
+        const int cnt = (int)(R - t0 < kTile ? R - t0 : kTile);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+            sc[0][k] = (float)coords[3 * (t0 + k)];
+            sc[1][k] = (float)coords[3 * (t0 + k) + 1];
+            sc[2][k] = (float)coords[3 * (t0 + k) + 2];
+        }
+        __syncthreads();
+        if (act) {
+            for (int k = 0; k < cnt; ++k) {
+                const float f0 = __fmul_rn(fabsf(__fsub_rn(p0, sc[0][k])), s0);
+                const float f1 = __fmul_rn(fabsf(__fsub_rn(p1, sc[1][k])), s1);
+                const float f2 = __fmul_rn(fabsf(__fsub_rn(p2, sc[2][k])), s2);
+                const float d = __fadd_rn(__fadd_rn(__fmul_rn(f0, f0), __fmul_rn(f1, f1)), __fmul_rn(f2, f2));
+                if (d < best) { best = d; bj = t0 + k; }
+            }
+        }
+    }
+    if (!act || R == 0) return;
+    float *v = dirs3 + 3 * i;
+    const float w0 = rdirs[3 * bj], w1 = rdirs[3 * bj + 1], w2 = rdirs[3 * bj + 2];
+    const float dot = __fadd_rn(__fadd_rn(__fmul_rn(v[0], w0), __fmul_rn(v[1], w1)), __fmul_rn(v[2], w2));
+    if (dot < 0.f) {
+        v[0] = -v[0];
+        v[1] = -v[1];
+        v[2] = -v[2];
+    }
+}
+
+inline int blocks1d(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(16 * kSMs, div_up(n, 256))); }
+
+}  // namespace
+}  // namespace m16
+
+using namespace m16;
+
+extern "C" int m16_detect_ridges(const float *resp, const float *quat3, int32_t d0, int32_t d1, int32_t d2,
+                                 double threshold, float *ridge, void *stream)
+{
+    if (d0 < 1 || d1 < 1 || d2 < 1 || d0 > 65535) return M16_ERR_BAD_SHAPE;
+    if (!resp || !quat3 || !ridge) return M16_ERR_BAD_ARG;
+    const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)d0);
+    dr_detect_ridges_kernel<<<grid, dim3(kBX, kBY, 1), 0, (cudaStream_t)stream>>>(resp, quat3, ridge, d0, d1, d2,
+                                                                                 threshold);
+    M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}
+
+extern "C" int m16_extract_main_directions(const float *quat3, int64_t n, float *dirs3, void *stream)
+{
+    if (n < 0 || (n > 0 && (!quat3 || !dirs3))) return M16_ERR_BAD_ARG;
+    if (n == 0) return M16_OK;
+    dr_extract_kernel<<<blocks1d(n), 256, 0, (cudaStream_t)stream>>>(quat3, dirs3, n);
+    M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}
+
+extern "C" int m16_complete_transformations(const float *dirs3, int64_t n, float *quat3, void *stream)
+{
+    if (n < 0 || (n > 0 && (!quat3 || !dirs3))) return M16_ERR_BAD_ARG;
+    if (n == 0) return M16_OK;
+    dr_complete_kernel<<<blocks1d(n), 256, 0, (cudaStream_t)stream>>>(dirs3, quat3, n);
+    M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}
+
+extern "C" int m16_adjust_nonridge_signs(float *dirs3, int32_t d0, int32_t d1, int32_t d2, const uint16_t *coords,
+                                         const float *rdirs, int64_t num_ridge, const double *scaling3,
+                                         void *stream)
+{
+    if (d0 < 1 || d1 < 1 || d2 < 1) return M16_ERR_BAD_SHAPE;
+    if (!dirs3 || !scaling3 || num_ridge < 1 || !coords || !rdirs) return M16_ERR_BAD_ARG;
+    const int64_t n = (int64_t)d0 * d1 * d2;
+    const int blocks = (int)div_up(n, 256);
+    dr_adjust_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(dirs3, coords, rdirs, num_ridge, d0, d1, d2,
+                                                               (float)scaling3[0], (float)scaling3[1],
+                                                               (float)scaling3[2]);
+    M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}

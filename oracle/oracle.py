@@ -89,6 +89,14 @@ def _declare_oracle(L):
     L.oracle_frangi.restype = None
     L.oracle_frangi.argtypes = [_i64, _i64, _i64, _vp, ctypes.c_int, _vp, _vp, ctypes.c_float, ctypes.c_float,
                                 ctypes.c_float, ctypes.c_int, _vp, _vp, _vp]
+    L.oracle_detect_ridges.restype = None
+    L.oracle_detect_ridges.argtypes = [_i64, _i64, _i64, ctypes.c_double, _vp, _vp, _vp]
+    L.oracle_extract_main_directions.restype = None
+    L.oracle_extract_main_directions.argtypes = [_i64, _vp, _vp]
+    L.oracle_complete_transformations.restype = None
+    L.oracle_complete_transformations.argtypes = [_i64, _vp, _vp]
+    L.oracle_adjust_nonridge_signs.restype = None
+    L.oracle_adjust_nonridge_signs.argtypes = [_i64, _i64, _i64, _vp, _vp, _vp, _i64, _vp]
     L.oracle_gvf_time_step.restype = ctypes.c_double
     L.oracle_gvf_time_step.argtypes = [_vp, ctypes.c_double, ctypes.c_int]
     L.oracle_gvf_run.restype = ctypes.c_int
@@ -433,3 +441,79 @@ def ref_frangi(img, scales, voxel_size=None, alpha=0.5, beta=0.5, c=None, bright
         R.ref_update_vesselness(ctypes.c_long(n), _ptr(val), _ptr(quat), _ptr(e), ctypes.c_float(0.5 if alpha is None else alpha),
                                 ctypes.c_float(beta), ctypes.c_float(cc), int(bool(bright)))
     return val, quat, np.array(cus, np.float32)
+
+
+# ----------------------------------------------------------------------------
+# direction kernels
+# ----------------------------------------------------------------------------
+
+def detect_ridges(resp, quat3, threshold):
+    resp = _f32(resp)
+    q = _f32(quat3)
+    out = np.empty_like(resp)
+    lib().oracle_detect_ridges(resp.shape[0], resp.shape[1], resp.shape[2], float(threshold), _ptr(out),
+                               _ptr(resp), _ptr(q))
+    return out
+
+
+def extract_main_directions(quat3):
+    q = _f32(quat3)
+    out = np.empty_like(q)
+    lib().oracle_extract_main_directions(q.size // 3, _ptr(out), _ptr(q))
+    return out
+
+
+def complete_transformations(dirs3):
+    d = _f32(dirs3)
+    out = np.empty_like(d)
+    lib().oracle_complete_transformations(d.size // 3, _ptr(out), _ptr(d))
+    return out
+
+
+def adjust_nonridge_signs(dirs3, coords, rdirs, scaling=(1, 1, 1)):
+    d = _f32(dirs3).copy()
+    c = np.require(coords, np.uint16, ["C", "A"])
+    r = _f32(rdirs)
+    sc = np.asarray(np.multiply(scaling, np.ones(3)), np.float32)
+    lib().oracle_adjust_nonridge_signs(d.shape[0], d.shape[1], d.shape[2], _ptr(d), _ptr(c), _ptr(r), len(c),
+                                       _ptr(sc))
+    return d
+
+
+def _image_8192(values, dtype):
+    """to_cl_image_8192 (cl_helpers.py:46-81) as the flat [row][8192][4] list."""
+    n = len(values)
+    rows = ((n - 1) >> 13) + 1
+    out = np.zeros((rows * 8192, 4), dtype)
+    out[:n, :3] = values
+    return out
+
+
+def ref_detect_ridges(resp, quat3, threshold):
+    resp = _f32(resp)
+    out = np.empty_like(resp)
+    ref().ref_detect_ridges(resp.shape[0], resp.shape[1], resp.shape[2], ctypes.c_double(threshold), _ptr(out),
+                            _ptr(resp), _ptr(_f32(quat3)))
+    return out
+
+
+def ref_extract_main_directions(quat3):
+    q = _f32(quat3).copy()
+    ref().ref_extract_main_directions(ctypes.c_long(q.size // 3), _ptr(q), _ptr(q))
+    return q
+
+
+def ref_complete_transformations(dirs3):
+    d = _f32(dirs3).copy()
+    ref().ref_complete_transformations(ctypes.c_long(d.size // 3), _ptr(d), _ptr(d))
+    return d
+
+
+def ref_adjust_nonridge_signs(dirs3, coords, rdirs, scaling=(1, 1, 1)):
+    d = _f32(dirs3).copy()
+    ci = _image_8192(np.asarray(coords), np.uint16)
+    di = _image_8192(np.asarray(rdirs), np.float32)
+    sc = np.asarray(np.multiply(scaling, np.ones(3)), np.float32)
+    ref().ref_adjust_nonridge_signs(d.shape[0], d.shape[1], d.shape[2], _ptr(d), _ptr(ci), _ptr(di), _ptr(sc),
+                                    len(coords))
+    return d

@@ -26,6 +26,13 @@ static inline float o_sq(float x) { return x * x; }
 /* OpenCL min(float, float): "returns y if y < x, otherwise x". */
 static inline float o_min(float x, float y) { return y < x ? y : x; }
 
+/* Float cosine and sine evaluated as the double function rounded to float:
+ * the correctly rounded value on every platform.  The reference's OpenCL
+ * cos(float) has implementation-defined accuracy and libm's cosf/sinf are not
+ * correctly rounded on every platform, so this is the portable reading. */
+static inline float o_cosf(float x) { return (float)cos((double)x); }
+static inline float o_sinf(float x) { return (float)sin((double)x); }
+
 /* qexpand, quaternion_math.h:79-90.  The half angles are (float sum) * 0.5
  * in double, stored to float; cos/sin of theta take a double argument. */
 static inline void o_qexpand(const float v[3], float q[4])
@@ -34,10 +41,10 @@ static inline void o_qexpand(const float v[3], float q[4])
     const float pm = (float)((double)(v[0] - v[2]) * 0.5);
     const float ct = (float)cos((double)v[1] * 0.5);
     const float st = (float)sin((double)v[1] * 0.5);
-    q[0] = cosf(pp) * ct;
-    q[1] = cosf(pm) * st;
-    q[2] = sinf(pm) * st;
-    q[3] = sinf(pp) * ct;
+    q[0] = o_cosf(pp) * ct;
+    q[1] = o_cosf(pm) * st;
+    q[2] = o_sinf(pm) * st;
+    q[3] = o_sinf(pp) * ct;
 }
 
 /* qrot, quaternion_math.h:114-147: out = q v q^-1 via two Hamilton

@@ -20,6 +20,17 @@
 #include <stddef.h>
 #include <string.h>
 
+/* cos/sin of a float as the double function rounded to float (correctly
+ * rounded on every platform; OpenCL leaves the accuracy of the float
+ * built-ins implementation-defined).  Double arguments keep the double
+ * functions. */
+static inline float shim_cos(float x) { return (float)cos((double)x); }
+static inline double shim_cos(double x) { return cos(x); }
+static inline float shim_sin(float x) { return (float)sin((double)x); }
+static inline double shim_sin(double x) { return sin(x); }
+#define cos(x) shim_cos(x)
+#define sin(x) shim_sin(x)
+
 #define __kernel
 #define __global
 #define __local

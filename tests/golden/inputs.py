@@ -103,3 +103,20 @@ def frangi_case(name):
 
 
 FRANGI_CASES = ("frangi_bright", "frangi_dark_aniso")
+
+
+def directions_case():
+    """Inputs of the direction-kernel fixture: response, squeezed quaternions,
+    vectors (with a zero vector), a ridge list with duplicate distances."""
+    rng = np.random.RandomState(41)
+    shape = (11, 14, 9)
+    resp = rng.uniform(0, 1, shape).astype(np.float32)
+    quats = random_squeezed(rng, shape)
+    vecs = rng.normal(size=shape + (3,)).astype(np.float32)
+    vecs[0, 0, 0] = 0.0
+    vecs[1, 2, 3] = (0.0, 0.0, 1.0)
+    R = 29
+    coords = np.stack([rng.randint(0, s, R) for s in shape], -1).astype(np.uint16)
+    coords[5] = coords[4] + np.array([2, 0, 0], np.uint16) if coords[4][0] + 2 < shape[0] else coords[5]
+    rdirs = rng.normal(size=(R, 3)).astype(np.float32)
+    return dict(resp=resp, quats=quats, vecs=vecs, coords=coords, rdirs=rdirs)

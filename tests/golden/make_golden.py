@@ -55,13 +55,29 @@ def make_frangi():
         print(name, val.shape, c, os.path.getsize(path))
 
 
+def make_directions():
+    d = I.directions_case()
+    out = {}
+    for th in (0.01, 0.3):
+        out["ridge_%g" % th] = O.ref_detect_ridges(d["resp"], d["quats"], th)
+    out["main"] = O.ref_extract_main_directions(d["quats"])
+    out["complete"] = O.ref_complete_transformations(d["vecs"])
+    out["adjust_iso"] = O.ref_adjust_nonridge_signs(d["vecs"], d["coords"], d["rdirs"], (1, 1, 1))
+    out["adjust_aniso"] = O.ref_adjust_nonridge_signs(d["vecs"], d["coords"], d["rdirs"], (1.5, 0.7, 1.2))
+    path = os.path.join(HERE, "directions.npz")
+    np.savez_compressed(path, **out)
+    print("directions", os.path.getsize(path))
+
+
 if __name__ == "__main__":
     if O.ref() is None:
         raise SystemExit("the reference checkout is needed to generate fixtures")
-    which = sys.argv[1:] or ["maxflow", "gvf", "frangi"]
+    which = sys.argv[1:] or ["maxflow", "gvf", "frangi", "directions"]
     if "maxflow" in which:
         make_maxflow()
     if "gvf" in which:
         make_gvf()
     if "frangi" in which:
         make_frangi()
+    if "directions" in which:
+        make_directions()

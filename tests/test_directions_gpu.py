@@ -1,0 +1,155 @@
+"""Parity of the CUDA direction kernels (csrc/directions.cu) and of the
+drop-in AdvancedAdjuster / TransformationCompleter with the oracle.
+
+The kernels follow the reference's rounding sequence (no contracted
+multiply-adds, the quaternion expansion's trigonometry in double), so the
+discrete outputs are compared exactly: ridge maps (at most 1e-4 of the voxels
+may differ through a last-bit difference of the device cos/sin), and the sign
+flips bit-exact given identical ridge inputs.  Completed frames are compared as
+rotations (1e-5)."""
+import io
+import contextlib
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+import inputs as I  # noqa: E402
+from oracle import adjust as A  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def _rot(sq):
+    phi, th, psi = [sq[..., k].astype(np.float64) for k in range(3)]
+    w = np.cos((phi + psi) / 2) * np.cos(th / 2)
+    x = np.cos((phi - psi) / 2) * np.sin(th / 2)
+    y = np.sin((phi - psi) / 2) * np.sin(th / 2)
+    z = np.sin((phi + psi) / 2) * np.cos(th / 2)
+    return np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                     2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                     2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1).reshape(-1, 3, 3)
+
+
+def _gpu_adjust(vecs, coords, rdirs, scaling):
+    import ctypes
+    import torch
+    from miccai2016_gb300 import _native as N
+    d = torch.from_numpy(np.ascontiguousarray(vecs)).cuda()
+    c = torch.from_numpy(np.ascontiguousarray(coords, np.uint16).view(np.int16)).cuda()
+    r = torch.from_numpy(np.ascontiguousarray(rdirs)).cuda()
+    sc = (ctypes.c_double * 3)(*scaling)
+    st = N.lib().m16_adjust_nonridge_signs(N.ptr(d), *vecs.shape[:3], N.ptr(c), N.ptr(r), len(coords), sc,
+                                          N.stream_ptr())
+    N.check("m16_adjust_nonridge_signs", st)
+    return d.cpu().numpy()
+
+
+def _gpu_extract(q):
+    import torch
+    from miccai2016_gb300 import _native as N
+    d = torch.from_numpy(np.ascontiguousarray(q)).cuda()
+    st = N.lib().m16_extract_main_directions(N.ptr(d), d.numel() // 3, N.ptr(d), N.stream_ptr())
+    N.check("m16_extract_main_directions", st)
+    return d.cpu().numpy()
+
+
+def test_golden_direction_kernels():
+    from miccai2016_gb300.adjust_directions import TransformationCompleter
+    from miccai2016_gb300.ridge_detection import RawRidgeDetector
+    d = I.directions_case()
+    g = np.load(os.path.join(HERE, "golden", "directions.npz"))
+    for th in (0.01, 0.3):
+        r = RawRidgeDetector(None, th).detect(d["resp"], d["quats"])
+        assert np.mean(r != g["ridge_%g" % th]) <= 1e-4
+    assert np.max(np.abs(_gpu_extract(d["quats"]) - g["main"])) <= 1e-6
+    comp = TransformationCompleter(d["vecs"]).complete()
+    assert np.max(np.abs(_rot(comp) - _rot(g["complete"]))) <= 1e-5
+    assert np.array_equal(_bits(_gpu_adjust(d["vecs"], d["coords"], d["rdirs"], (1, 1, 1))), _bits(g["adjust_iso"]))
+    assert np.array_equal(_bits(_gpu_adjust(d["vecs"], d["coords"], d["rdirs"], (1.5, 0.7, 1.2))),
+                          _bits(g["adjust_aniso"]))
+
+
+@pytest.mark.parametrize("shape", [(40, 33, 50), (7, 64, 3), (1, 20, 20)])
+def test_kernels_match_oracle_on_random_inputs(shape):
+    from miccai2016_gb300.ridge_detection import RawRidgeDetector
+    rng = np.random.RandomState(sum(shape))
+    resp = rng.uniform(0, 1, shape).astype(np.float32)
+    q = I.random_squeezed(rng, shape)
+    r = RawRidgeDetector(None, 0.05).detect(resp, q)
+    assert np.mean(r != O.detect_ridges(resp, q, 0.05)) <= 1e-4
+    assert np.max(np.abs(_gpu_extract(q) - O.extract_main_directions(q))) <= 1e-6
+    v = rng.normal(size=shape + (3,)).astype(np.float32)
+    R = 300
+    coords = np.stack([rng.randint(0, s, R) for s in shape], -1).astype(np.uint16)
+    rd = rng.normal(size=(R, 3)).astype(np.float32)
+    for sc in [(1, 1, 1), (0.5, 2.0, 1.25)]:
+        assert np.array_equal(_bits(_gpu_adjust(v, coords, rd, sc)), _bits(O.adjust_nonridge_signs(v, coords, rd, sc)))
+
+
+def test_nearest_ridge_ties_go_to_the_lowest_index():
+    shape = (1, 1, 5)
+    v = np.tile(np.array([1, 0, 0], np.float32), (1, 1, 5, 1))
+    coords = np.array([[0, 0, 0], [0, 0, 4], [0, 0, 2]], np.uint16)
+    rd = np.array([[1, 0, 0], [-1, 0, 0], [-1, 0, 0]], np.float32)
+    out = _gpu_adjust(v, coords, rd, (1, 1, 1))
+    # voxel 1 is equidistant (1) from points 0 and 2 -> point 0 wins, keeps its sign
+    # voxel 3 is equidistant from points 1 and 2 -> point 1 wins, flips
+    assert out[0, 0, 1, 0] == 1 and out[0, 0, 3, 0] == -1
+    assert np.array_equal(_bits(out), _bits(O.adjust_nonridge_signs(v, coords, rd, (1, 1, 1))))
+
+
+def _small_tube():
+    from miccai2016_gb300 import phantom as P
+    noisy, truth = P.helix_phantom((32, 40, 40), 2.0, 10.0, 16.0, 0.3, 7)
+    val, quat, _ = O.frangi(noisy, (1, 2, 2))
+    resp = ((val - val.min()) / (val.max() - val.min())).astype(np.float32)
+    return resp, quat
+
+
+def test_advanced_adjuster_matches_oracle():
+    from miccai2016_gb300.adjust_directions import AdvancedAdjuster
+    resp, quat = _small_tube()
+    th = (0.2, 0.5)
+    with contextlib.redirect_stdout(io.StringIO()):
+        adj_o, ridge_o, main_o = A.advanced_adjuster(quat, resp, th)
+        obj = AdvancedAdjuster(th, quat, resp, voxel_size=(1, 1, 1))
+        adj = obj.execute(verbose=False)
+    assert 0 < ridge_o.sum() < 3000
+    same_main = _bits(obj.main_dirs_unadjusted) == _bits(main_o)
+    assert np.mean(~same_main) <= 1e-4
+    assert np.max(np.abs(obj.main_dirs_unadjusted - main_o)) <= 1e-6
+    assert np.mean(obj.ridge != ridge_o) <= 1e-4
+    if np.array_equal(obj.ridge, ridge_o):
+        # identical ridge: every sign identical, and the bits wherever the
+        # main direction itself has identical bits
+        assert np.all(np.sum(adj * adj_o, axis=-1) > 0)
+        vox = np.all(same_main, axis=-1)
+        assert np.array_equal(_bits(adj)[vox], _bits(adj_o)[vox])
+
+
+def test_ridge_detection_only_and_no_cleaning():
+    from miccai2016_gb300.adjust_directions import AdvancedAdjuster
+    resp, quat = _small_tube()
+    obj = AdvancedAdjuster(0.3, quat, resp, ridge_detection_only=True, clean_ridge=False)
+    assert obj.execute(verbose=False) is None
+    assert np.mean(obj.ridge != O.detect_ridges(resp, quat, 0.3)) <= 1e-4
+
+
+def test_completer_round_trip_keeps_the_main_direction():
+    from miccai2016_gb300.adjust_directions import TransformationCompleter
+    rng = np.random.RandomState(9)
+    v = rng.normal(size=(10, 11, 12, 3)).astype(np.float32)
+    q = TransformationCompleter(v).complete()
+    back = _gpu_extract(q)
+    vn = v / np.linalg.norm(v, axis=-1, keepdims=True)
+    assert np.max(np.abs(back - vn)) <= 1e-5

@@ -1,0 +1,119 @@
+"""The direction-kernel oracle (oracle/directions.c) against golden fixtures
+from the reference's detect_ridges.cl / adjust_directions.cl and live against
+them; the host-logic restatements (hysteresis, minimum spanning tree, ridge
+cleaning) against the reference's literal algorithms.  CPU only."""
+import io
+import contextlib
+import os
+import sys
+
+import numpy as np
+import pytest
+from scipy.sparse.csgraph import minimum_spanning_tree
+from scipy.spatial.distance import pdist, squareform
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+from oracle import adjust as A  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+import inputs as I  # noqa: E402
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def test_direction_kernels_match_golden():
+    d = I.directions_case()
+    g = np.load(os.path.join(HERE, "golden", "directions.npz"))
+    for th in (0.01, 0.3):
+        assert np.array_equal(O.detect_ridges(d["resp"], d["quats"], th), g["ridge_%g" % th])
+    assert np.array_equal(_bits(O.extract_main_directions(d["quats"])), _bits(g["main"]))
+    assert np.array_equal(_bits(O.complete_transformations(d["vecs"])), _bits(g["complete"]))
+    assert np.array_equal(_bits(O.adjust_nonridge_signs(d["vecs"], d["coords"], d["rdirs"], (1, 1, 1))),
+                          _bits(g["adjust_iso"]))
+    assert np.array_equal(_bits(O.adjust_nonridge_signs(d["vecs"], d["coords"], d["rdirs"], (1.5, 0.7, 1.2))),
+                          _bits(g["adjust_aniso"]))
+
+
+@pytest.mark.parametrize("shape", [(5, 7, 9), (16, 12, 20), (1, 6, 5)])
+def test_direction_kernels_match_reference(has_ref, shape):
+    if not has_ref:
+        pytest.skip("reference checkout not present")
+    rng = np.random.RandomState(sum(shape))
+    resp = rng.uniform(0, 1, shape).astype(np.float32)
+    q = I.random_squeezed(rng, shape)
+    for th in (0.01, 0.5):
+        assert np.array_equal(O.detect_ridges(resp, q, th), O.ref_detect_ridges(resp, q, th))
+    assert np.array_equal(_bits(O.extract_main_directions(q)), _bits(O.ref_extract_main_directions(q)))
+    v = rng.normal(size=shape + (3,)).astype(np.float32)
+    assert np.array_equal(_bits(O.complete_transformations(v)), _bits(O.ref_complete_transformations(v)))
+    R = 17
+    coords = np.stack([rng.randint(0, s, R) for s in shape], -1).astype(np.uint16)
+    rd = rng.normal(size=(R, 3)).astype(np.float32)
+    for sc in [(1, 1, 1), (0.5, 2.0, 1.25)]:
+        assert np.array_equal(_bits(O.adjust_nonridge_signs(v, coords, rd, sc)),
+                              _bits(O.ref_adjust_nonridge_signs(v, coords, rd, sc)))
+
+
+def test_label_hysteresis_equals_the_reference_flood_fill():
+    from miccai2016_gb300.ridge_detection import hysteresis_threshold
+    rng = np.random.RandomState(2)
+    for t in range(30):
+        shape = tuple(rng.randint(3, 14, 3))
+        cand = rng.uniform(size=shape) < rng.uniform(0.1, 0.5)
+        sure = cand & (rng.uniform(size=shape) < 0.1)
+        if t % 5 == 0:
+            sure |= rng.uniform(size=shape) < 0.02   # sure voxels outside the candidates
+        a = A.hysteresis_threshold(cand.copy(), sure.copy())
+        b = hysteresis_threshold(cand.copy(), sure.copy())
+        assert np.array_equal(a, b)
+
+
+def test_stable_mst_is_scipys_tree_when_distances_are_distinct():
+    rng = np.random.RandomState(3)
+    for _ in range(5):
+        pts = rng.uniform(0, 50, (300, 3))
+        d = pdist(pts)
+        assert len(np.unique(d)) == len(d)
+        ref = minimum_spanning_tree(squareform(d)).tocoo()
+        ours = A.stable_mst(pts, (1, 1, 1)).tocoo()
+        e1 = set(zip(np.minimum(ref.row, ref.col), np.maximum(ref.row, ref.col)))
+        e2 = set(zip(np.minimum(ours.row, ours.col), np.maximum(ours.row, ours.col)))
+        assert e1 == e2
+
+
+@pytest.mark.parametrize("vs", [(1, 1, 1), (1.5, 0.7, 1.2), (1, 1, 3)])
+def test_sparse_mst_equals_the_dense_stable_kruskal(vs):
+    from miccai2016_gb300.ridge_mst import ridge_mst_edges
+    rng = np.random.RandomState(int(sum(vs) * 10))
+    for _ in range(4):
+        pts = np.unique(np.concatenate([rng.randint(0, 10, (120, 3)) + rng.randint(0, 35, 3) for _ in range(4)]), axis=0)
+        pts = pts[rng.permutation(len(pts))]
+        a, b = ridge_mst_edges(pts, vs)
+        t = A.stable_mst(pts, vs).tocoo()
+        assert set(zip(np.minimum(a, b), np.maximum(a, b))) == set(zip(np.minimum(t.row, t.col),
+                                                                       np.maximum(t.row, t.col)))
+
+
+def test_ridge_directions_and_cleaning_match_the_reference_logic():
+    from miccai2016_gb300.adjust_directions import AdvancedAdjuster
+    rng = np.random.RandomState(4)
+    shape = (24, 24, 24)
+    ridge = np.zeros(shape, np.float32)
+    # a few short 26-connected curves and specks
+    for _ in range(6):
+        p = rng.randint(2, 22, 3)
+        for _ in range(rng.randint(1, 25)):
+            ridge[tuple(np.clip(p, 0, 23))] = 1
+            p = p + rng.randint(-1, 2, 3)
+    main = rng.normal(size=shape + (3,)).astype(np.float32)
+    obj = AdvancedAdjuster((0.01, 0.3), np.zeros(shape + (3,), np.float32), np.zeros(shape, np.float32))
+    c1, d1 = A.adjust_ridge_directions(ridge, main, (1.0, 1.0, 1.0))
+    c2, d2 = obj._adjust_ridge_directions(ridge, main)
+    assert np.array_equal(c1, c2) and np.array_equal(_bits(d1), _bits(d2))
+    with contextlib.redirect_stdout(io.StringIO()):
+        k1 = A.clean_ridge(ridge, c1, d1, (1.0, 1.0, 1.0))
+        k2 = obj._do_clean_ridge(ridge, c2, d2)
+    assert np.array_equal(k1, k2)
