@@ -352,9 +352,91 @@ def run_ours(args, cfg):
                              "sample": sample},
             "clocks": clocks, "dice_fast": dice,
             "voxel_iterations_per_s": value * n * cfg["num_iter"]}
+    if cfg["name"] == "plain256":   # the default workload also reports the batched grid search
+        line["batched"] = run_batched_grid()
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def run_batched_grid(plain_sample=17):
+    """The batched grid search (one m16_batch_solve over all 425 ATV
+    instances of a 128^3 volume, each stopping at residual 1e-4) against the
+    plain one-solve-per-call path on a sample of the same instances."""
+    import torch
+    from miccai2016_gb300 import phantom as P, pipeline
+    from miccai2016_gb300.batched import BatchedCut
+    from miccai2016_gb300.continuous_cut_anisotropic_gpu import CmfCutQAnisotropicGpu
+    cfg = P.CONFIG_GRID_128
+    noisy, truth = P.helix_phantom(cfg["shape"], cfg["tube_radius"], cfg["helix_radius"], cfg["pitch"],
+                                   cfg["sigma"], cfg["seed"])
+    t0 = time.perf_counter()
+    cut, stages = pipeline.prepare_cut_inputs(noisy, cfg["sigma"], scales=cfg["scales"], gvf_mu=cfg["gvf_mu"],
+                                              gvf_iterations=cfg["gvf_iter"])
+    prep_s = time.perf_counter() - t0
+    bp = BatchedCut.CutParameters()
+    bp.num_iter, bp.update, bp.error_bound = cfg["num_iter"], cfg["update"], cfg["error_bound"]
+    bc = BatchedCut(bp)
+    vol = bc.prepare_volume(noisy, cut["quats"], cut["fgw"], cut["bgw"], grad2=cut["grad2"])
+    grid = [(w, d) for w in cfg["weightings"] for d in cfg["decays"]]
+    insts = [dict(volume=0, weighting=w, decay=d, eigs=P.ATV_EIGS) for (w, d) in grid]
+    # warm-up: a two-instance batch loads the kernels
+    wp = BatchedCut.CutParameters()
+    wp.num_iter, wp.update, wp.error_bound = 60, 30, -1.0
+    BatchedCut(wp).solve([vol], insts[:2])
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    us = bc.solve([vol], insts)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_s = e0.elapsed_time(e1) / 1000.0
+    iters = bc.last_iterations.copy()
+    truth_d = torch.from_numpy(truth).cuda()
+    tsum = float(truth_d.sum())
+    dice_b = np.array([float(2 * ((u >= 0.5) * truth_d).sum() / ((u >= 0.5).sum() + tsum)) for u in us])
+    del us
+    best = int(np.argmax(dice_b))
+    # plain path on a sample: the decays of the best weighting (17 instances)
+    wi = best // len(cfg["decays"])
+    sample = [wi * len(cfg["decays"]) + k for k in range(len(cfg["decays"]))][:plain_sample]
+    cp = CmfCutQAnisotropicGpu.CutParameters()
+    cp.num_iter, cp.update, cp.error_bound = cfg["num_iter"], cfg["update"], cfg["error_bound"]
+    cutter = CmfCutQAnisotropicGpu(cp)
+    d_img, d_q = vol["img"], vol["quats"]
+    alphas = [torch.from_numpy(P.nonterminal_weights(cut["grad2_f64"], grid[k][0], grid[k][1]).astype(np.float32))
+              .cuda() for k in sample]
+    cutter.execute(d_img, d_q, P.ATV_EIGS, alphas[0], vol["cs"], vol["ct"], verbose=False)   # warm-up
+    torch.cuda.synchronize()
+    e0.record(stream)
+    plain_u = []
+    plain_iters = []
+    for k, a in zip(sample, alphas):
+        plain_u.append(cutter.execute(d_img, d_q, P.ATV_EIGS, a, vol["cs"], vol["ct"], verbose=False))
+        plain_iters.append(cutter.last_iterations)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_s = e0.elapsed_time(e1) / 1000.0
+    dice_p = np.array([float(2 * ((u >= 0.5) * truth_d).sum() / ((u >= 0.5).sum() + tsum)) for u in plain_u])
+    n_vox = int(np.prod(cfg["shape"]))
+    vox_it = float(np.sum(iters)) * n_vox
+    batched_rate = len(insts) / batched_s
+    plain_rate = len(sample) / plain_s
+    return {"workload": "425-instance ATV grid search (25 weightings x 17 decays), 128x128x128 helix, "
+                        "noise sigma 1.5, stop at residual 1e-4 (update 30, at most 3000 iterations)",
+            "solves_per_s": batched_rate, "plain_solves_per_s": plain_rate,
+            "speedup_vs_plain": batched_rate / plain_rate,
+            "plain_sample": "the 17 decays of the best weighting, one CmfCutQAnisotropicGpu.execute() each",
+            "batched_s": batched_s, "plain_sample_s": plain_s,
+            "iterations": {"min": int(iters.min()), "median": float(np.median(iters)), "max": int(iters.max())},
+            "voxel_iterations_per_s": vox_it / batched_s,
+            "achieved_gbs_state": 60.0 * vox_it / batched_s / 1e9,
+            "best_dice_fast": float(dice_b[best]), "best_weighting": grid[best][0], "best_decay": grid[best][1],
+            "max_dice_diff_vs_plain": float(np.max(np.abs(dice_b[sample] - dice_p))),
+            "iteration_diff_vs_plain": int(np.max(np.abs(iters[sample] - np.asarray(plain_iters)))),
+            "shared_preparation_s": prep_s, "preparation_stages_s": stages,
+            "ridge_points": cut["ridge_points"]}
 
 
 def main():

@@ -138,6 +138,47 @@ int m16_maxflow_solve_static(const float *img, const float *quat3, const double 
                              float *u, int32_t *iterations, double *residuals, int32_t residuals_cap,
                              int32_t *n_residuals, void *stream);
 
+/* ---- batched max-flow -------------------------------------------------------
+ * Replaces the reference's one-execute()-per-grid-point loop
+ * (src/phantom_experiment.py:350-368) by one batch: instances over any set of
+ * volumes, each with its own (weighting, decay) or alpha field and its own
+ * constant eigenvalues, advanced together and stopped one by one.          */
+typedef struct m16_batch_volume {
+    int32_t d0, d1, d2, reserved;
+    const float *img;     /* N: u of every instance starts as img / (max(img) + FLT_MIN) */
+    const float *quat3;   /* N x 3 squeezed quaternions */
+    const float *grad2;   /* N: |grad img|^2 for alpha = weighting * exp(-grad2 / decay^2), or NULL */
+    const float *cs;      /* N source capacities */
+    const float *ct;      /* N sink capacities */
+    double scaling[3];    /* voxel size [mm/voxel] */
+} m16_batch_volume;
+
+typedef struct m16_batch_instance {
+    int32_t volume;       /* index into the volume array */
+    int32_t reserved;
+    double weighting;     /* alpha = weighting * exp(-grad2 / decay^2) (phantom_experiment.py:359) ... */
+    double decay;
+    const float *alpha;   /* ... unless this per-voxel alpha (N) is given */
+    double sqevals[3];    /* square roots of the constant eigenvalues, e.g. ATV (1, 10^-0.75, 10^-0.75) */
+    float *u;             /* N output */
+} m16_batch_instance;
+
+/* Workspace bytes of m16_batch_solve (0 when the descriptors are invalid). */
+size_t m16_batch_workspace_bytes(const m16_batch_volume *vols, int32_t nvol, const m16_batch_instance *inst,
+                                 int32_t ninst);
+
+/*
+ * Solve every instance as m16_maxflow_solve would (same iteration, same
+ * residual and stopping rule from params; params->scaling is ignored, each
+ * volume carries its own).  iterations and residuals (host, ninst each,
+ * optional) receive each instance's iteration count and last residual.
+ * stats (host, optional) counts launches and, with time_kernels, the summed
+ * device time of the batched flow/label launches.  Synchronizes `stream`.
+ */
+int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const m16_batch_instance *inst, int32_t ninst,
+                    const m16_cut_params *params, int32_t *iterations, double *residuals, void *workspace,
+                    size_t workspace_bytes, void *stream, m16_solve_stats *stats);
+
 /* ---- gradient vector flow --------------------------------------------------
  * Workspace bytes of m16_gvf_run; has_response says whether a response field
  * will be passed, mags_cap bounds the convergence log (maxiter / update + 1). */

@@ -55,6 +55,18 @@ class SolveStats(ctypes.Structure):
                 ("p_ms", _f64), ("u_ms", _f64)]
 
 
+class BatchVolume(ctypes.Structure):
+    """m16_batch_volume (include/miccai2016_gb300.h)."""
+    _fields_ = [("d0", _i32), ("d1", _i32), ("d2", _i32), ("reserved", _i32), ("img", _vp), ("quat3", _vp),
+                ("grad2", _vp), ("cs", _vp), ("ct", _vp), ("scaling", _f64 * 3)]
+
+
+class BatchInstance(ctypes.Structure):
+    """m16_batch_instance (include/miccai2016_gb300.h)."""
+    _fields_ = [("volume", _i32), ("reserved", _i32), ("weighting", _f64), ("decay", _f64), ("alpha", _vp),
+                ("sqevals", _f64 * 3), ("u", _vp)]
+
+
 def _declare(L):
     L.m16_status_string.restype = ctypes.c_char_p
     L.m16_status_string.argtypes = [ctypes.c_int]
@@ -85,6 +97,11 @@ def _declare(L):
     L.m16_complete_transformations.argtypes = [_vp, _i64, _vp, _vp]
     L.m16_adjust_nonridge_signs.restype = ctypes.c_int
     L.m16_adjust_nonridge_signs.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp, _i64, _vp, _vp]
+    L.m16_batch_workspace_bytes.restype = _sz
+    L.m16_batch_workspace_bytes.argtypes = [ctypes.POINTER(BatchVolume), _i32, ctypes.POINTER(BatchInstance), _i32]
+    L.m16_batch_solve.restype = ctypes.c_int
+    L.m16_batch_solve.argtypes = [ctypes.POINTER(BatchVolume), _i32, ctypes.POINTER(BatchInstance), _i32,
+                                  ctypes.POINTER(CutParams), _vp, _vp, _vp, _sz, _vp, ctypes.POINTER(SolveStats)]
     L.m16_gvf_workspace_bytes.restype = _sz
     L.m16_gvf_workspace_bytes.argtypes = [_i32, _i32, _i32, _i32, _i32]
     L.m16_gvf_run.restype = ctypes.c_int

@@ -133,7 +133,9 @@ class AdvancedAdjuster(TreePrintable):
         adjusted = None
         if (not self.ridge_detection_only) or self.clean_ridge:
             main_dirs = self._qeigs_to_main_dirs()
-            ridge_coords, ridge_dirs = self._adjust_ridge_directions(labeled_ridge, main_dirs)
+            # before cleaning, only the per-segment norms matter (see _adjust_ridge_directions)
+            ridge_coords, ridge_dirs = self._adjust_ridge_directions(labeled_ridge, main_dirs,
+                                                                     join_components=not self.clean_ridge)
             if self.clean_ridge:
                 labeled_ridge = self._do_clean_ridge(labeled_ridge, ridge_coords, ridge_dirs)
                 if not self.ridge_detection_only:
@@ -187,16 +189,19 @@ class AdvancedAdjuster(TreePrintable):
         self.__main_dirs_unadjusted = main_dirs.copy()
         return main_dirs
 
-    def _adjust_ridge_directions(self, labeled_ridge, main_dirs):
+    def _adjust_ridge_directions(self, labeled_ridge, main_dirs, join_components=True):
         """MST over the ridge points, sign propagation from point 0
         (adjust_directions.py:365-417).  Returns (coords uint16 R x 3,
         directions float32 R x 3).  The tree is SciPy's Kruskal tree with
         equal distances taken in (i, j) order, computed without the dense
-        distance matrix (ridge_mst.py)."""
+        distance matrix (ridge_mst.py).  join_components=False leaves out the
+        MST edges between groups of points more than one step apart, so each
+        group keeps its own global sign; the cleaning only uses per-segment
+        norms of sums, which that sign does not change."""
         coords = np.argwhere(labeled_ridge)   # C order, as zip(*np.where(...))
         if len(coords) == 0:
             raise ValueError("no ridge points: nothing to propagate directions along")
-        a, b = ridge_mst_edges(coords, self.voxel_size)
+        a, b = ridge_mst_edges(coords, self.voxel_size, join_components=join_components)
         dirs = main_dirs[coords[:, 0], coords[:, 1], coords[:, 2]]
         adjusted = propagate_signs(len(coords), a, b, dirs)
         return np.asarray(coords, dtype=np.uint16, order="C"), adjusted

@@ -1,0 +1,89 @@
+"""
+Batched ATV max-flow: many CmfCutQAnisotropicGpu solves advanced together in
+one launch per sweep (csrc/batched.cu, m16_batch_solve).
+
+The reference's grid search (src/phantom_experiment.py:350-368) calls
+CmfCutQAnisotropicGpu.execute() once per (weighting, decay) and cut type with
+alpha = weighting * exp(-|grad I|^2 / decay^2) computed on the host.  Here a
+batch holds any number of volumes and instances; an instance names its volume,
+its (weighting, decay) -- alpha is then computed in the flow sweep from the
+volume's |grad I|^2 -- or an explicit alpha field, and its constant
+eigenvalues.  Each instance stops on its own at the residual threshold.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+from .continuous_cut_anisotropic_gpu import CmfCutQAnisotropicGpu
+
+
+class BatchedCut(object):
+    """Batch solver with the cut parameters of CmfCutQAnisotropicGpu.CutParameters."""
+
+    CutParameters = CmfCutQAnisotropicGpu.CutParameters
+
+    def __init__(self, params):
+        self.params = params
+        self.last_iterations = None
+        self.last_residuals = None
+        self.last_stats = None
+        self._ws = None
+
+    def prepare_volume(self, img, quats, cs, ct, grad2=None, scaling=None):
+        """Device copies of one volume's inputs (img, squeezed quaternions,
+        capacities and, for (weighting, decay) instances, |grad img|^2)."""
+        shape = tuple(int(s) for s in img.shape)
+        return dict(shape=shape, img=N.to_device_f32(img, shape), quats=N.to_device_f32(quats, shape + (3,)),
+                    cs=N.to_device_f32(cs, shape), ct=N.to_device_f32(ct, shape),
+                    grad2=None if grad2 is None else N.to_device_f32(grad2, shape),
+                    scaling=(1.0, 1.0, 1.0) if scaling is None else tuple(float(v) for v in scaling))
+
+    def solve(self, volumes, instances, time_kernels=False):
+        """volumes: list of prepare_volume() dicts; instances: list of dicts
+        with 'volume' (index), 'eigs' (3 constant eigenvalues) and either
+        ('weighting', 'decay') or 'alpha' (an array of the volume's shape).
+        Returns the list of u (CUDA tensors) in instance order."""
+        torch = N.torch_mod()
+        L = N.lib()
+        nv, ni = len(volumes), len(instances)
+        vd = (N.BatchVolume * nv)()
+        for k, v in enumerate(volumes):
+            d0, d1, d2 = v["shape"]
+            vd[k] = N.BatchVolume(d0, d1, d2, 0, N.ptr(v["img"]), N.ptr(v["quats"]), N.ptr(v["grad2"]),
+                                  N.ptr(v["cs"]), N.ptr(v["ct"]), (ctypes.c_double * 3)(*v["scaling"]))
+        us, keep = [], []
+        idesc = (N.BatchInstance * ni)()
+        for k, inst in enumerate(instances):
+            shape = volumes[inst["volume"]]["shape"]
+            u = torch.empty(shape, dtype=torch.float32, device=N.device())
+            us.append(u)
+            alpha = inst.get("alpha")
+            if alpha is not None:
+                alpha = N.to_device_f32(alpha, shape)
+                keep.append(alpha)
+            sq = np.sqrt(np.asarray(inst["eigs"], dtype=np.float64))
+            idesc[k] = N.BatchInstance(int(inst["volume"]), 0, float(inst.get("weighting", 0.0)),
+                                       float(inst.get("decay", 0.0)), N.ptr(alpha), (ctypes.c_double * 3)(*sq),
+                                       N.ptr(u))
+        p = self.params
+        cp = N.CutParams(float(p.cc), float(p.steps), float(p.error_bound), int(p.num_iter), int(p.update),
+                         (ctypes.c_double * 3)(1.0, 1.0, 1.0))
+        nbytes = L.m16_batch_workspace_bytes(vd, nv, idesc, ni)
+        if nbytes == 0:
+            raise ValueError("invalid batch description")
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = None
+            self._ws = N.workspace(nbytes)
+        iters = (ctypes.c_int32 * ni)()
+        res = (ctypes.c_double * ni)()
+        stats = N.SolveStats(int(bool(time_kernels)), 0, 0, 0, 0.0, 0.0)
+        st = L.m16_batch_solve(vd, nv, idesc, ni, ctypes.byref(cp), iters, res, N.ptr(self._ws), self._ws.numel(),
+                               N.stream_ptr(), ctypes.byref(stats))
+        N.check("m16_batch_solve", st)
+        self.last_iterations = np.array(iters[:], np.int64)
+        self.last_residuals = np.array(res[:], np.float64)
+        self.last_stats = stats
+        return us

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "sweeps.cuh"
 
 namespace m16 {
 namespace {
@@ -113,19 +114,33 @@ __global__ void mf_init_kernel(MfArgs a, const float *__restrict__ img, const fl
     }
 }
 
-// ---- P: flow update and projection (update_qp.cl:150-232) -----------------
-//
-// Each thread walks its z-column in batches of kZB slices: all loads of a
-// batch are issued before any arithmetic, so every thread keeps ~10 kZB
-// independent loads in flight (the sweeps are memory-latency bound otherwise).
+// ---- P and U sweeps (bodies in sweeps.cuh, shared with the batched engine) --
 
-#ifndef M16_MF_ZB
-#define M16_MF_ZB 2
-#endif
 #ifndef M16_MF_MINB
 #define M16_MF_MINB 1
 #endif
-constexpr int kZB = M16_MF_ZB;
+constexpr int kZB = kMfZB;
+
+__device__ __forceinline__ FlowView flow_view(const MfArgs &a)
+{
+    FlowView f;
+    f.d0 = a.d0; f.d1 = a.d1; f.d2 = a.d2;
+    f.ss0 = a.ss0; f.ss1 = a.ss1; f.ss2 = a.ss2;
+    f.sq0 = a.sq0; f.sq1 = a.sq1; f.sq2 = a.sq2; f.isq0 = a.isq0; f.isq1 = a.isq1; f.isq2 = a.isq2;
+    f.alpha_scalar = a.alpha_scalar; f.alpha = a.alpha; f.grad2 = nullptr; f.w = 0.f; f.neg_inv_decay2 = 0.f;
+    f.sqeigs = a.sqeigs; f.q4 = a.q4; f.tmp = a.tmp; f.hp0 = a.hp0; f.hp1 = a.hp1; f.hp2 = a.hp2;
+    return f;
+}
+
+__device__ __forceinline__ LabelView label_view(const MfArgs &a)
+{
+    LabelView l;
+    l.d0 = a.d0; l.d1 = a.d1; l.d2 = a.d2;
+    l.rcc = a.rcc; l.rs0 = a.rs0; l.rs1 = a.rs1; l.rs2 = a.rs2;
+    l.hp0 = a.hp0; l.hp1 = a.hp1; l.hp2 = a.hp2; l.cs = a.cs; l.ct = a.ct; l.labels = a.labels;
+    l.pt = a.pt; l.u = a.u; l.tmp = a.tmp;
+    return l;
+}
 
 template <bool POINTWISE, bool ALPHA_ARR>
 __global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_p_kernel(MfArgs a)
@@ -135,68 +150,8 @@ __global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_p_kernel(MfA
     const int y = blockIdx.y * kBY + threadIdx.y;
     if (x >= a.d2 || y >= a.d1) return;
     const int z0 = blockIdx.z * a.zc;
-    const int z1 = min(z0 + a.zc, a.d0);
-    const int64_t s0 = (int64_t)a.d1 * a.d2;
-    int64_t i = ((int64_t)z0 * a.d1 + y) * a.d2 + x;
-    const bool yin = y < a.d1 - 1, xin = x < a.d2 - 1;
-    float t = __ldg(a.tmp + i);
-    for (int zb = z0; zb < z1; zb += kZB, i += kZB * s0) {
-        float tz[kZB], ty[kZB], tx[kZB], al[kZB], h0[kZB], h1[kZB], h2[kZB];
-        float4 q[kZB];
-        float se0[kZB], se1[kZB], se2[kZB];
-#pragma unroll
-        for (int k = 0; k < kZB; ++k) {
-            if (zb + k < z1) {
-                const int64_t j = i + k * s0;
-                tz[k] = (zb + k < a.d0 - 1) ? __ldg(a.tmp + j + s0) : 0.f;
-                ty[k] = yin ? __ldg(a.tmp + j + a.d2) : 0.f;
-                tx[k] = xin ? __ldg(a.tmp + j + 1) : 0.f;
-                q[k] = __ldg(a.q4 + j);
-                al[k] = ALPHA_ARR ? __ldg(a.alpha + j) : a.alpha_scalar;
-                h0[k] = a.hp0[j];
-                h1[k] = a.hp1[j];
-                h2[k] = a.hp2[j];
-                if (POINTWISE) {
-                    se0[k] = __ldg(a.sqeigs + 3 * j);
-                    se1[k] = __ldg(a.sqeigs + 3 * j + 1);
-                    se2[k] = __ldg(a.sqeigs + 3 * j + 2);
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < kZB; ++k) {
-            if (zb + k < z1) {
-                const int64_t j = i + k * s0;
-                const float tc = k == 0 ? t : tz[k - 1];
-                const bool zin = zb + k < a.d0 - 1;
-                const float3 g = make_float3(zin ? (tz[k] - tc) * a.ss0 : 0.f, yin ? (ty[k] - tc) * a.ss1 : 0.f,
-                                             xin ? (tx[k] - tc) * a.ss2 : 0.f);
-                const Rot R = quat2rot(q[k]);
-                float s0v = a.sq0, s1v = a.sq1, s2v = a.sq2, i0v = a.isq0, i1v = a.isq1, i2v = a.isq2;
-                if (POINTWISE) {
-                    s0v = se0[k]; s1v = se1[k]; s2v = se2[k];
-                    i0v = 1.f / s0v; i1v = 1.f / s1v; i2v = 1.f / s2v;
-                }
-                // p = H^-1 hp + H^T (steps grad tmp) with H = R diag(sqrt eig)
-                const float3 rg = rot_t(R, g);
-                const float3 rh = rot_t(R, make_float3(h0[k], h1[k], h2[k]));
-                float3 p = make_float3(rh.x * i0v + rg.x * s0v, rh.y * i1v + rg.y * s1v,
-                                       rh.z * i2v + rg.z * s2v);
-                // project onto |p| <= alpha, then hp = H p
-                const float nrm = sqrtf(p.x * p.x + p.y * p.y + p.z * p.z);
-                const float sc = nrm > al[k] ? al[k] / nrm : 1.f;
-                p = make_float3(p.x * sc * s0v, p.y * sc * s1v, p.z * sc * s2v);
-                const float3 h = rot(R, p);
-                a.hp0[j] = h.x;
-                a.hp1[j] = h.y;
-                a.hp2[j] = h.z;
-            }
-        }
-        t = tz[kZB - 1];
-    }
+    flow_column<POINTWISE, ALPHA_ARR ? kAlphaArray : kAlphaScalar>(flow_view(a), x, y, z0, min(z0 + a.zc, a.d0));
 }
-
-// ---- U: divergence, terminal flows, labels (update_qp.cl:241-300, 311-316) -
 
 template <bool SUPERVISED, bool CHECK>
 __global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_u_kernel(MfArgs a)
@@ -208,61 +163,7 @@ __global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_u_kernel(MfA
     float acc = 0.f;
     if (x < a.d2 && y < a.d1) {
         const int z0 = blockIdx.z * a.zc;
-        const int z1 = min(z0 + a.zc, a.d0);
-        const int64_t s0 = (int64_t)a.d1 * a.d2;
-        int64_t i = ((int64_t)z0 * a.d1 + y) * a.d2 + x;
-        const bool ylo = y > 0, xlo = x > 0, yhi = y < a.d1 - 1, xhi = x < a.d2 - 1;
-        float h0m = z0 > 0 ? __ldg(a.hp0 + i - s0) : 0.f;
-        for (int zb = z0; zb < z1; zb += kZB, i += kZB * s0) {
-            float h0[kZB], h1[kZB], h2[kZB], h1m[kZB], h2m[kZB], uo[kZB], ptv[kZB], csv[kZB], ctv[kZB];
-            uint8_t lab[kZB];
-#pragma unroll
-            for (int k = 0; k < kZB; ++k) {
-                if (zb + k < z1) {
-                    const int64_t j = i + k * s0;
-                    h0[k] = __ldg(a.hp0 + j);
-                    h1[k] = __ldg(a.hp1 + j);
-                    h2[k] = __ldg(a.hp2 + j);
-                    h1m[k] = ylo ? __ldg(a.hp1 + j - a.d2) : 0.f;
-                    h2m[k] = xlo ? __ldg(a.hp2 + j - 1) : 0.f;
-                    uo[k] = a.u[j];
-                    ptv[k] = a.pt[j];
-                    csv[k] = __ldg(a.cs + j);
-                    ctv[k] = __ldg(a.ct + j);
-                    if (SUPERVISED) lab[k] = __ldg(a.labels + j);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < kZB; ++k) {
-                if (zb + k < z1) {
-                    const int64_t j = i + k * s0;
-                    const int z = zb + k;
-                    const float prev0 = k == 0 ? h0m : h0[k - 1];
-                    const float a0 = (z < a.d0 - 1 ? h0[k] : 0.f) - (z > 0 ? prev0 : 0.f);
-                    const float a1 = (yhi ? h1[k] : 0.f) - h1m[k];
-                    const float a2 = (xhi ? h2[k] : 0.f) - h2m[k];
-                    const float div = a0 * a.rs0 + a1 * a.rs1 + a2 * a.rs2;
-                    // p_s = min(div + p_t - (u - s_off)/cc, C_s); p_t = min(-div + p_s + (u - t_off)/cc, C_t)
-                    // with (s_off, t_off) = (1, 0) unsupervised and (!(l & 2), l & 1) with seeds l
-                    float s_off = 1.f, t_off = 0.f;
-                    if (SUPERVISED) {
-                        s_off = (float)(!(lab[k] & 2));
-                        t_off = (float)(lab[k] & 1);
-                    }
-                    const float psx = div + ptv[k] - a.rcc * (uo[k] - s_off);
-                    const float ps = csv[k] < psx ? csv[k] : psx;
-                    const float ptx = -div + ps + a.rcc * (uo[k] - t_off);
-                    const float ptn = ctv[k] < ptx ? ctv[k] : ptx;
-                    const float err = div - ps + ptn;
-                    const float un = uo[k] - err / a.rcc;
-                    a.pt[j] = ptn;
-                    a.u[j] = un;
-                    a.tmp[j] = err - un * a.rcc;
-                    if (CHECK) acc += fabsf(err);
-                }
-            }
-            h0m = h0[kZB - 1];
-        }
+        acc = label_column<SUPERVISED>(label_view(a), x, y, z0, min(z0 + a.zc, a.d0));
     }
     if (CHECK) {
         const float s = block_sum(acc, red);

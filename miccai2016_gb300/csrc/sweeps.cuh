@@ -1,0 +1,178 @@
+// sweeps.cuh -- the two per-iteration sweeps of the ATV continuous max-flow,
+// shared by the single-solve path (maxflow.cu) and the batched engine
+// (batched.cu).  One thread walks one (y, x) column from z0 to z1; see
+// maxflow.cu for the reference equations (src/clcode-anisotropic/update_qp.cl).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "common.cuh"
+
+#ifndef M16_MF_ZB
+#define M16_MF_ZB 2
+#endif
+
+namespace m16 {
+
+constexpr int kMfZB = M16_MF_ZB;   // z-slices whose loads are issued together
+
+// where the projection radius alpha comes from
+enum AlphaMode { kAlphaScalar = 0, kAlphaArray = 1, kAlphaFromGrad2 = 2 };
+
+// Everything one instance's flow sweep reads and writes.
+struct FlowView {
+    int d0, d1, d2;
+    float ss0, ss1, ss2;                       // steps / voxel size, scaled (SS0-2)
+    float sq0, sq1, sq2, isq0, isq1, isq2;     // sqrt of the constant eigenvalues and reciprocals
+    float alpha_scalar;                        // kAlphaScalar
+    const float *alpha;                        // kAlphaArray
+    const float *grad2;                        // kAlphaFromGrad2: alpha = w * exp(-grad2 / decay^2)
+    float w, neg_inv_decay2;
+    const float *sqeigs;                       // per-voxel sqrt eigenvalues (POINTWISE)
+    const float4 *q4;                          // expanded quaternions
+    const float *tmp;
+    float *hp0, *hp1, *hp2;
+};
+
+// Everything one instance's label sweep reads and writes.
+struct LabelView {
+    int d0, d1, d2;
+    float rcc, rs0, rs1, rs2;
+    const float *hp0, *hp1, *hp2;
+    const float *cs, *ct;
+    const uint8_t *labels;
+    float *pt, *u, *tmp;
+};
+
+// P: p = H^-1 hp + H^T (steps grad tmp), projected onto |p| <= alpha, hp = H p
+// (update_qp.cl:150-232) for voxels (z0..z1, y, x).
+template <bool POINTWISE, int ALPHA>
+__device__ __forceinline__ void flow_column(const FlowView &a, int x, int y, int z0, int z1)
+{
+    const int64_t s0 = (int64_t)a.d1 * a.d2;
+    int64_t i = ((int64_t)z0 * a.d1 + y) * a.d2 + x;
+    const bool yin = y < a.d1 - 1, xin = x < a.d2 - 1;
+    float t = __ldg(a.tmp + i);
+    for (int zb = z0; zb < z1; zb += kMfZB, i += kMfZB * s0) {
+        float tz[kMfZB], ty[kMfZB], tx[kMfZB], al[kMfZB], h0[kMfZB], h1[kMfZB], h2[kMfZB];
+        float4 q[kMfZB];
+        float se0[kMfZB], se1[kMfZB], se2[kMfZB];
+#pragma unroll
+        for (int k = 0; k < kMfZB; ++k) {
+            if (zb + k < z1) {
+                const int64_t j = i + k * s0;
+                tz[k] = (zb + k < a.d0 - 1) ? __ldg(a.tmp + j + s0) : 0.f;
+                ty[k] = yin ? __ldg(a.tmp + j + a.d2) : 0.f;
+                tx[k] = xin ? __ldg(a.tmp + j + 1) : 0.f;
+                q[k] = __ldg(a.q4 + j);
+                if (ALPHA == kAlphaArray) al[k] = __ldg(a.alpha + j);
+                else if (ALPHA == kAlphaFromGrad2) al[k] = __ldg(a.grad2 + j);
+                else al[k] = a.alpha_scalar;
+                h0[k] = a.hp0[j];
+                h1[k] = a.hp1[j];
+                h2[k] = a.hp2[j];
+                if (POINTWISE) {
+                    se0[k] = __ldg(a.sqeigs + 3 * j);
+                    se1[k] = __ldg(a.sqeigs + 3 * j + 1);
+                    se2[k] = __ldg(a.sqeigs + 3 * j + 2);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kMfZB; ++k) {
+            if (zb + k < z1) {
+                const int64_t j = i + k * s0;
+                const float tc = k == 0 ? t : tz[k - 1];
+                const bool zin = zb + k < a.d0 - 1;
+                const float3 g = make_float3(zin ? (tz[k] - tc) * a.ss0 : 0.f, yin ? (ty[k] - tc) * a.ss1 : 0.f,
+                                             xin ? (tx[k] - tc) * a.ss2 : 0.f);
+                const Rot R = quat2rot(q[k]);
+                float s0v = a.sq0, s1v = a.sq1, s2v = a.sq2, i0v = a.isq0, i1v = a.isq1, i2v = a.isq2;
+                if (POINTWISE) {
+                    s0v = se0[k]; s1v = se1[k]; s2v = se2[k];
+                    i0v = 1.f / s0v; i1v = 1.f / s1v; i2v = 1.f / s2v;
+                }
+                const float rad = ALPHA == kAlphaFromGrad2 ? a.w * expf(a.neg_inv_decay2 * al[k]) : al[k];
+                const float3 rg = rot_t(R, g);
+                const float3 rh = rot_t(R, make_float3(h0[k], h1[k], h2[k]));
+                float3 p = make_float3(rh.x * i0v + rg.x * s0v, rh.y * i1v + rg.y * s1v,
+                                       rh.z * i2v + rg.z * s2v);
+                const float nrm = sqrtf(p.x * p.x + p.y * p.y + p.z * p.z);
+                const float sc = nrm > rad ? rad / nrm : 1.f;
+                p = make_float3(p.x * sc * s0v, p.y * sc * s1v, p.z * sc * s2v);
+                const float3 h = rot(R, p);
+                a.hp0[j] = h.x;
+                a.hp1[j] = h.y;
+                a.hp2[j] = h.z;
+            }
+        }
+        t = tz[kMfZB - 1];
+    }
+}
+
+// U: div(hp), p_s, p_t, u, and tmp = err - u / cc (update_qp.cl:241-300 with
+// update_tmp :311-316 fused) for voxels (z0..z1, y, x); returns sum |err|.
+template <bool SUPERVISED>
+__device__ __forceinline__ float label_column(const LabelView &a, int x, int y, int z0, int z1)
+{
+    float acc = 0.f;
+    const int64_t s0 = (int64_t)a.d1 * a.d2;
+    int64_t i = ((int64_t)z0 * a.d1 + y) * a.d2 + x;
+    const bool ylo = y > 0, xlo = x > 0, yhi = y < a.d1 - 1, xhi = x < a.d2 - 1;
+    float h0m = z0 > 0 ? __ldg(a.hp0 + i - s0) : 0.f;
+    for (int zb = z0; zb < z1; zb += kMfZB, i += kMfZB * s0) {
+        float h0[kMfZB], h1[kMfZB], h2[kMfZB], h1m[kMfZB], h2m[kMfZB], uo[kMfZB], ptv[kMfZB], csv[kMfZB],
+            ctv[kMfZB];
+        uint8_t lab[kMfZB];
+#pragma unroll
+        for (int k = 0; k < kMfZB; ++k) {
+            if (zb + k < z1) {
+                const int64_t j = i + k * s0;
+                h0[k] = __ldg(a.hp0 + j);
+                h1[k] = __ldg(a.hp1 + j);
+                h2[k] = __ldg(a.hp2 + j);
+                h1m[k] = ylo ? __ldg(a.hp1 + j - a.d2) : 0.f;
+                h2m[k] = xlo ? __ldg(a.hp2 + j - 1) : 0.f;
+                uo[k] = a.u[j];
+                ptv[k] = a.pt[j];
+                csv[k] = __ldg(a.cs + j);
+                ctv[k] = __ldg(a.ct + j);
+                if (SUPERVISED) lab[k] = __ldg(a.labels + j);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kMfZB; ++k) {
+            if (zb + k < z1) {
+                const int64_t j = i + k * s0;
+                const int z = zb + k;
+                const float prev0 = k == 0 ? h0m : h0[k - 1];
+                const float a0 = (z < a.d0 - 1 ? h0[k] : 0.f) - (z > 0 ? prev0 : 0.f);
+                const float a1 = (yhi ? h1[k] : 0.f) - h1m[k];
+                const float a2 = (xhi ? h2[k] : 0.f) - h2m[k];
+                const float div = a0 * a.rs0 + a1 * a.rs1 + a2 * a.rs2;
+                // p_s = min(div + p_t - (u - s_off)/cc, C_s); p_t = min(-div + p_s + (u - t_off)/cc, C_t)
+                // with (s_off, t_off) = (1, 0) unsupervised and (!(l & 2), l & 1) with seeds l
+                float s_off = 1.f, t_off = 0.f;
+                if (SUPERVISED) {
+                    s_off = (float)(!(lab[k] & 2));
+                    t_off = (float)(lab[k] & 1);
+                }
+                const float psx = div + ptv[k] - a.rcc * (uo[k] - s_off);
+                const float ps = csv[k] < psx ? csv[k] : psx;
+                const float ptx = -div + ps + a.rcc * (uo[k] - t_off);
+                const float ptn = ctv[k] < ptx ? ctv[k] : ptx;
+                const float err = div - ps + ptn;
+                const float un = uo[k] - err / a.rcc;
+                a.pt[j] = ptn;
+                a.u[j] = un;
+                a.tmp[j] = err - un * a.rcc;
+                acc += fabsf(err);
+            }
+        }
+        h0m = h0[kMfZB - 1];
+    }
+    return acc;
+}
+
+}  // namespace m16

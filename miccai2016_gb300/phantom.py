@@ -190,5 +190,10 @@ CONFIG_PLAIN_256 = dict(shape=(256, 256, 256), tube_radius=12.0, helix_radius=64
                         seed=0, weighting=10 ** -1.25, decay=10 ** 1.5, num_iter=1000, gvf_iter=100, gvf_mu=0.2)
 CONFIG_PLAIN_128 = dict(shape=(128, 128, 128), tube_radius=6.0, helix_radius=32.0, pitch=40.0, sigma=1.0,
                         seed=0, weighting=10 ** -1.25, decay=10 ** 1.5, num_iter=300, gvf_iter=100, gvf_mu=0.2)
+# the batched grid search: 25 weightings x 17 decays (phantom_experiment.py:167-168)
+CONFIG_GRID_128 = dict(shape=(128, 128, 128), tube_radius=6.0, helix_radius=32.0, pitch=40.0, sigma=1.5, seed=0,
+                       scales=(2, 6, 3), gvf_mu=0.2, gvf_iter=100, num_iter=3000, update=30, error_bound=1e-4,
+                       weightings=tuple(float(w) for w in __import__("numpy").logspace(-2.5, 0.5, 25)),
+                       decays=tuple(float(d) for d in __import__("numpy").logspace(-1, 3, 17)))
 ATV_EIGS = (1.0, 10 ** -1.5, 10 ** -1.5)   # phantom_experiment.py:154, 362
 TV_EIGS = (1.0, 1.0, 1.0)

@@ -53,9 +53,13 @@ def _kruskal_by_order(n, i, j, order_keys):
     return t.row.astype(np.int64), t.col.astype(np.int64)
 
 
-def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0)):
+def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True):
     """Edges (a, b) of the (weight, i, j)-ordered Euclidean MST of integer
-    points (R x 3, axis order 0, 1, 2) with per-axis voxel size."""
+    points (R x 3, axis order 0, 1, 2) with per-axis voxel size.  With
+    join_components=False only the local phase runs: the result is the MST
+    minus its edges longer than r, i.e. a spanning tree of every group of
+    points linked by steps not longer than r (each 26-connected set lies in
+    one such group)."""
     pts = np.asarray(points, dtype=np.int64)
     R = len(pts)
     if R < 2:
@@ -95,7 +99,7 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0)):
     # global phase: join the local trees
     forest = scipy.sparse.coo_matrix((np.ones(len(ta)), (ta, tb)), shape=(R, R))
     ncomp, comp = connected_components(forest, directed=False)
-    if ncomp == 1:
+    if ncomp == 1 or not join_components:
         return ta, tb
     members = [np.nonzero(comp == c)[0] for c in range(ncomp)]
     trees = [cKDTree(u[m]) for m in members]
@@ -132,15 +136,29 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0)):
 def propagate_signs(n, edges_a, edges_b, dirs, root=0):
     """Sign propagation along the tree from `root` (adjust_directions.py:382-415):
     a child keeps its direction if its dot product with its parent's adjusted
-    direction is >= 0, else it is negated.  Unreached points stay NaN."""
+    direction is >= 0, else it is negated.  When the edges form a forest,
+    every other tree is propagated from its lowest-index point, as if that
+    point were the root."""
     adjusted = np.ones((n, 3), dtype=np.float32) * np.float32(np.nan)
-    adjusted[root] = dirs[root]
-    if n == 1:
-        return adjusted
     g = scipy.sparse.coo_matrix((np.ones(len(edges_a)), (edges_a, edges_b)), shape=(n, n)).tocsr()
+    ncomp, comp = connected_components(g, directed=False)
+    # the other trees hang off `root` through virtual edges to their
+    # lowest-index points, which restart the propagation
+    _, first = np.unique(comp, return_index=True)
+    starts = np.asarray([f for f in first if comp[f] != comp[root]], np.int64)
+    if len(starts):
+        va = np.concatenate([edges_a, np.full(len(starts), root, np.int64)])
+        vb = np.concatenate([edges_b, starts])
+        g = scipy.sparse.coo_matrix((np.ones(len(va)), (va, vb)), shape=(n, n)).tocsr()
+    restart = np.zeros(n, bool)
+    restart[starts] = True
+    adjusted[root] = dirs[root]
     order, pred = breadth_first_order(g, root, directed=False, return_predecessors=True)
     for c in order[1:]:
         cur = dirs[c]
+        if restart[c]:
+            adjusted[c] = cur
+            continue
         ref = adjusted[pred[c]]
         adjusted[c] = cur if np.dot(cur, ref) >= 0 else -cur
     return adjusted

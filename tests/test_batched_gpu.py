@@ -1,0 +1,90 @@
+"""The batched engine (csrc/batched.cu) against individual plain solves: every
+instance of a batch gives the u of CmfCutQAnisotropicGpu.execute() on the same
+inputs within the max-flow tolerance (1e-3 max-abs after a fixed iteration
+count; alpha is computed in float on the device instead of float64 on the
+host), and stops at the same check."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+U_TOL = 1e-3
+
+
+def _volume(seed, shape):
+    from miccai2016_gb300 import phantom as P
+    rng = np.random.RandomState(seed)
+    img = rng.normal(0.5, 0.6, shape).astype(np.float32)
+    q = np.stack([rng.uniform(-np.pi, np.pi, shape), rng.uniform(0, np.pi, shape),
+                  rng.uniform(-np.pi, np.pi, shape)], -1).astype(np.float32)
+    bgw, fgw = P.bgfg_weights(img, 0.8)
+    grad2 = P.grad_mag_sq(img)
+    return dict(img=img, quats=q, cs=fgw.astype(np.float32), ct=bgw.astype(np.float32),
+                grad2=grad2.astype(np.float32), grad2_f64=grad2)
+
+
+def _plain(v, inst, num_iter, update, error_bound):
+    from miccai2016_gb300 import phantom as P
+    from miccai2016_gb300.continuous_cut_anisotropic_gpu import CmfCutQAnisotropicGpu
+    p = CmfCutQAnisotropicGpu.CutParameters()
+    p.num_iter, p.update, p.error_bound = num_iter, update, error_bound
+    c = CmfCutQAnisotropicGpu(p)
+    alpha = inst.get("alpha")
+    if alpha is None:
+        alpha = P.nonterminal_weights(v["grad2_f64"], inst["weighting"], inst["decay"]).astype(np.float32)
+    u = c.execute(v["img"], v["quats"], inst["eigs"], alpha, v["cs"], v["ct"], verbose=False)
+    return u, c.last_iterations
+
+
+def _batch(vols, insts, num_iter, update, error_bound):
+    from miccai2016_gb300.batched import BatchedCut
+    p = BatchedCut.CutParameters()
+    p.num_iter, p.update, p.error_bound = num_iter, update, error_bound
+    b = BatchedCut(p)
+    dv = [b.prepare_volume(v["img"], v["quats"], v["cs"], v["ct"], grad2=v["grad2"]) for v in vols]
+    us = b.solve(dv, insts)
+    return [u.cpu().numpy() for u in us], b.last_iterations
+
+
+ATV = (1.0, 10 ** -1.5, 10 ** -1.5)
+TV = (1.0, 1.0, 1.0)
+
+
+def test_mixed_batch_matches_plain_solves():
+    vols = [_volume(1, (24, 20, 36)), _volume(2, (17, 33, 9))]
+    insts = [dict(volume=0, weighting=10 ** -1.25, decay=10 ** 1.5, eigs=ATV),
+             dict(volume=0, weighting=10 ** -2.0, decay=1.0, eigs=TV),
+             dict(volume=1, weighting=0.3, decay=3.0, eigs=ATV),
+             dict(volume=0, weighting=0.05, decay=0.5, eigs=ATV),
+             dict(volume=1, alpha=np.full((17, 33, 9), 0.07, np.float32), eigs=TV),
+             dict(volume=1, weighting=1.0, decay=100.0, eigs=(1.0, 0.5, 0.25))]
+    us, its = _batch(vols, insts, 120, 30, -1.0)
+    for k, inst in enumerate(insts):
+        u, it = _plain(vols[inst["volume"]], inst, 120, 30, -1.0)
+        assert its[k] == it == 120
+        assert np.max(np.abs(us[k] - u)) <= U_TOL, k
+
+
+def test_instances_stop_on_their_own():
+    vols = [_volume(3, (32, 32, 32))]
+    insts = [dict(volume=0, weighting=w, decay=d, eigs=e) for w in (0.01, 0.1, 1.0) for d in (1.0, 30.0)
+             for e in (ATV, TV)]
+    us, its = _batch(vols, insts, 2000, 10, 2e-3)
+    assert len(set(its.tolist())) > 1          # they do not all stop together
+    for k, inst in enumerate(insts):
+        u, it = _plain(vols[0], inst, 2000, 10, 2e-3)
+        assert abs(int(its[k]) - it) <= 10
+        if int(its[k]) == it:
+            assert np.max(np.abs(us[k] - u)) <= U_TOL
+
+
+def test_grid_search_shape_of_the_reference():
+    """25 x 17 (weighting, decay) points on one volume, as phantom_experiment.py:167-168."""
+    vols = [_volume(4, (16, 16, 16))]
+    ws = np.logspace(-2.5, 0.5, 25)
+    ds = np.logspace(-1, 3, 17)
+    insts = [dict(volume=0, weighting=w, decay=d, eigs=ATV) for w in ws for d in ds]
+    us, its = _batch(vols, insts, 60, 30, -1.0)
+    assert len(us) == 425 and np.all(its == 60)
+    for k in (0, 200, 424):
+        u, _ = _plain(vols[0], insts[k], 60, 30, -1.0)
+        assert np.max(np.abs(us[k] - u)) <= U_TOL

@@ -117,3 +117,25 @@ def test_ridge_directions_and_cleaning_match_the_reference_logic():
         k1 = A.clean_ridge(ridge, c1, d1, (1.0, 1.0, 1.0))
         k2 = obj._do_clean_ridge(ridge, c2, d2)
     assert np.array_equal(k1, k2)
+
+
+def test_cleaning_is_the_same_without_joining_the_segments():
+    from miccai2016_gb300.adjust_directions import AdvancedAdjuster
+    rng = np.random.RandomState(11)
+    shape = (30, 30, 30)
+    ridge = np.zeros(shape, np.float32)
+    for _ in range(12):
+        p = rng.randint(2, 28, 3)
+        for _ in range(rng.randint(1, 30)):
+            ridge[tuple(np.clip(p, 0, 29))] = 1
+            p = p + rng.randint(-1, 2, 3)
+    main = rng.normal(size=shape + (3,)).astype(np.float32)
+    obj = AdvancedAdjuster((0.01, 0.3), np.zeros(shape + (3,), np.float32), np.zeros(shape, np.float32))
+    c1, d1 = obj._adjust_ridge_directions(ridge, main, join_components=True)
+    c2, d2 = obj._adjust_ridge_directions(ridge, main, join_components=False)
+    with contextlib.redirect_stdout(io.StringIO()):
+        k1 = A.clean_ridge(ridge, c1, d1, (1.0, 1.0, 1.0))
+        k2 = obj._do_clean_ridge(ridge, c2, d2)
+    assert np.array_equal(k1, k2)
+    # every point's direction is the joined one up to one sign per segment
+    assert np.allclose(np.abs(d1), np.abs(d2))
