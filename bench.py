@@ -10,9 +10,10 @@ iterations (residual checked every 30).  One step = one solve.
   value  solves/s with the inputs resident in HBM (all ranks summed)
   e2e    solves/s through the drop-in CmfCutQAnisotropicGpu.execute() with
          pinned host inputs: H2D of the inputs and D2H of u inside every step
-  roofline  the flow (P) and label (U) kernels' launch times, measured with
-         CUDA events on the solve's stream during the timed region, against
-         the algorithmic bytes of one launch (P 44 B, U 40 B per voxel)
+  roofline  the flow sweep (the dominant kernel of an iteration: flow 44 B,
+         labels 40 B per voxel), its launch time measured with CUDA events on
+         the solve's stream in a second pass over the same solves; the fused
+         one-launch iteration (84 B per voxel) is timed once beside it
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun every rank runs its own replica (the solves are independent).
@@ -36,6 +37,7 @@ sys.path.insert(0, ROOT)
 METRIC = "ATV max-flow solves/s batched+served vs plain at equal Dice; p50/p99 latency"
 P_BYTES = 44   # flow sweep: tmp 4 + quat 12 + alpha 4 + hp 12 read, hp 12 written
 U_BYTES = 40   # label sweep: hp 12 + cs 4 + ct 4 + pt 4 + u 4 read, pt 4 + u 4 + tmp 4 written
+F_BYTES = 84   # one iteration (flow + labels), the algorithmic bytes per voxel-iteration
 
 
 def _rank_info():
@@ -260,7 +262,7 @@ def run_ours(args, cfg):
     launches = 0
     ev0.record(stream)
     for _ in range(args.steps):
-        s = N.SolveStats(0, 0, 0, 0, 0.0, 0.0)
+        s = N.SolveStats(0, 0, 0, 0, 0.0, 0.0, 0, 0)
         solve(s)
         launches += s.launches
     ev1.record(stream)
@@ -268,14 +270,18 @@ def run_ours(args, cfg):
     if dist:
         dist.barrier()
     ms = ev0.elapsed_time(ev1)
-    # the same solves again with every flow/label launch bracketed by CUDA
+    # the same solves again with every flow / label launch bracketed by CUDA
     # events on the solve's stream: the per-kernel times of the roofline
     p_ms = u_ms = 0.0
     p_n = u_n = 0
     for _ in range(args.steps):
-        s = N.SolveStats(1, 0, 0, 0, 0.0, 0.0)
+        s = N.SolveStats(1, 0, 0, 0, 0.0, 0.0, N.PATH_DEFAULT, 0)
         solve(s)
         p_ms += s.p_ms; u_ms += s.u_ms; p_n += s.p_launches; u_n += s.u_launches
+    # and once with the fused iteration (one launch per iteration) for comparison
+    s2 = N.SolveStats(1, 0, 0, 0, 0.0, 0.0, N.PATH_FUSED, 0)
+    solve(s2)
+    fused_ms, fused_n = s2.p_ms, s2.p_launches
     torch.cuda.synchronize()
     clocks = sampler.stop() if sampler else None
     if dist:
@@ -321,25 +327,31 @@ def run_ours(args, cfg):
             dist.destroy_process_group()
         return
     peak, peak_kind = _peaks()
+    f_avg = fused_ms / max(fused_n, 1)
+    f_gbs = F_BYTES * n / (f_avg * 1e-3) / 1e9
     p_avg = p_ms / max(p_n, 1)
     u_avg = u_ms / max(u_n, 1)
     p_gbs = P_BYTES * n / (p_avg * 1e-3) / 1e9
     u_gbs = U_BYTES * n / (u_avg * 1e-3) / 1e9
-    dom = "p" if p_ms >= u_ms else "u"
     traffic = _traffic_summary()
     tr = None
     if traffic:
-        key = "mf_update_p" if dom == "p" else "mf_update_u"
-        ent = traffic.get(key)
+        ent = traffic.get("mf_update_p")
         if ent and ent.get("voxels"):
             tr = float(ent["dram_bytes_per_launch"]) * n / float(ent["voxels"])
-    roof = {"bound": "hbm", "kernel": "mf_update_p (flow sweep)" if dom == "p" else "mf_update_u (label sweep)",
-            "achieved": p_gbs if dom == "p" else u_gbs, "peak": peak, "unit": "GB/s",
-            "frac": (p_gbs if dom == "p" else u_gbs) / peak, "peak_kind": peak_kind, "traffic": tr,
-            "algorithmic_bytes_per_launch": (P_BYTES if dom == "p" else U_BYTES) * n,
-            "avg_launch_ms": p_avg if dom == "p" else u_avg}
-    kernels = {"mf_update_p": {"avg_ms": p_avg, "launches": p_n, "GB/s": p_gbs, "frac": p_gbs / peak},
-               "mf_update_u": {"avg_ms": u_avg, "launches": u_n, "GB/s": u_gbs, "frac": u_gbs / peak}}
+    # the dominant kernel of the default (two-sweep) iteration is the flow sweep
+    roof = {"bound": "hbm", "kernel": "mf_update_p_kernel (flow sweep of one max-flow iteration)",
+            "achieved": p_gbs, "peak": peak, "unit": "GB/s", "frac": p_gbs / peak, "peak_kind": peak_kind,
+            "traffic": tr, "algorithmic_bytes_per_launch": P_BYTES * n, "avg_launch_ms": p_avg}
+    it_ms = p_avg + u_avg
+    kernels = {"mf_update_p": {"avg_ms": p_avg, "launches": p_n, "GB/s": p_gbs, "frac": p_gbs / peak,
+                               "bytes_per_voxel": P_BYTES},
+               "mf_update_u": {"avg_ms": u_avg, "launches": u_n, "GB/s": u_gbs, "frac": u_gbs / peak,
+                               "bytes_per_voxel": U_BYTES},
+               "iteration": {"ms": it_ms, "GB/s": F_BYTES * n / (it_ms * 1e-3) / 1e9,
+                             "frac": F_BYTES * n / (it_ms * 1e-3) / 1e9 / peak, "bytes_per_voxel": F_BYTES},
+               "fused_path": {"mf_fused_kernel_avg_ms": f_avg, "launches": fused_n, "GB/s": f_gbs,
+                              "frac": f_gbs / peak, "bytes_per_voxel": F_BYTES}}
     cpu_v, kind, cpu_dt, sample = cpu_baseline(cfg, inp, iters=args.ref_iters)
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -431,7 +443,7 @@ def run_batched_grid(plain_sample=17):
             "batched_s": batched_s, "plain_sample_s": plain_s,
             "iterations": {"min": int(iters.min()), "median": float(np.median(iters)), "max": int(iters.max())},
             "voxel_iterations_per_s": vox_it / batched_s,
-            "achieved_gbs_state": 60.0 * vox_it / batched_s / 1e9,
+            "achieved_gbs_state": 60.0 * vox_it / batched_s / 1e9,   # flow 28 + label 32 B of state per voxel-iteration
             "best_dice_fast": float(dice_b[best]), "best_weighting": grid[best][0], "best_decay": grid[best][1],
             "max_dice_diff_vs_plain": float(np.max(np.abs(dice_b[sample] - dice_p))),
             "iteration_diff_vs_plain": int(np.max(np.abs(iters[sample] - np.asarray(plain_iters)))),

@@ -90,14 +90,27 @@ int m16_maxflow_solve(const float *img, const float *quat3, const double *sqeval
                       float *u, int32_t *iterations, double *residuals, int32_t residuals_cap,
                       int32_t *n_residuals, void *workspace, size_t workspace_bytes, void *stream);
 
+/* Iteration paths of the single solve.  TWO_SWEEPS: a flow launch, then a
+ * label launch; FUSED: one launch per iteration (flow and labels of a 32 x 8
+ * x z tile together, the flow field and tmp double-buffered).  Both do the
+ * same per-voxel arithmetic; DEFAULT is the one measured faster on sm_103a
+ * (two sweeps).  The workspace size reported by m16_maxflow_workspace_bytes
+ * covers both. */
+#define M16_PATH_DEFAULT 0
+#define M16_PATH_TWO_SWEEPS 1
+#define M16_PATH_FUSED 2
+
 /* Counters of one solve, for benchmarks and tracing. */
 typedef struct m16_solve_stats {
     int32_t time_kernels;  /* in: 1 brackets every flow/label kernel launch with CUDA events */
     int32_t launches;      /* out: kernels the call launched */
     int32_t p_launches;    /* out: flow (P) kernel launches that ran */
     int32_t u_launches;    /* out: label (U) kernel launches that ran */
-    double p_ms;           /* out: summed device time of the P launches (time_kernels only) */
+    double p_ms;           /* out: summed device time of the P launches, or of the fused
+                              iteration launches (time_kernels only) */
     double u_ms;           /* out: summed device time of the U launches (time_kernels only) */
+    int32_t path;          /* in: M16_PATH_* -- how an iteration is launched */
+    int32_t reserved;
 } m16_solve_stats;
 
 /* m16_maxflow_solve with counters; stats (host) may be NULL. */

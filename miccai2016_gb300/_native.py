@@ -49,10 +49,14 @@ class CutParams(ctypes.Structure):
                 ("update", _i32), ("scaling", _f64 * 3)]
 
 
+# iteration paths of the single solve (m16_solve_stats.path)
+PATH_DEFAULT, PATH_TWO_SWEEPS, PATH_FUSED = 0, 1, 2
+
+
 class SolveStats(ctypes.Structure):
     """m16_solve_stats (include/miccai2016_gb300.h)."""
     _fields_ = [("time_kernels", _i32), ("launches", _i32), ("p_launches", _i32), ("u_launches", _i32),
-                ("p_ms", _f64), ("u_ms", _f64)]
+                ("p_ms", _f64), ("u_ms", _f64), ("path", _i32), ("reserved", _i32)]
 
 
 class BatchVolume(ctypes.Structure):

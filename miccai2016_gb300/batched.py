@@ -41,10 +41,13 @@ class BatchedCut(object):
                     grad2=None if grad2 is None else N.to_device_f32(grad2, shape),
                     scaling=(1.0, 1.0, 1.0) if scaling is None else tuple(float(v) for v in scaling))
 
-    def solve(self, volumes, instances, time_kernels=False):
+    def solve(self, volumes, instances, time_kernels=False, path=None):
         """volumes: list of prepare_volume() dicts; instances: list of dicts
         with 'volume' (index), 'eigs' (3 constant eigenvalues) and either
         ('weighting', 'decay') or 'alpha' (an array of the volume's shape).
+        path is accepted for symmetry with the single solve; the batched
+        engine has one iteration path (flow and label sweeps over groups of
+        four interleaved instances).
         Returns the list of u (CUDA tensors) in instance order."""
         torch = N.torch_mod()
         L = N.lib()
@@ -79,7 +82,8 @@ class BatchedCut(object):
             self._ws = N.workspace(nbytes)
         iters = (ctypes.c_int32 * ni)()
         res = (ctypes.c_double * ni)()
-        stats = N.SolveStats(int(bool(time_kernels)), 0, 0, 0, 0.0, 0.0)
+        stats = N.SolveStats(int(bool(time_kernels)), 0, 0, 0, 0.0, 0.0,
+                             N.PATH_DEFAULT if path is None else int(path), 0)
         st = L.m16_batch_solve(vd, nv, idesc, ni, ctypes.byref(cp), iters, res, N.ptr(self._ws), self._ws.numel(),
                                N.stream_ptr(), ctypes.byref(stats))
         N.check("m16_batch_solve", st)
@@ -87,3 +91,60 @@ class BatchedCut(object):
         self.last_residuals = np.array(res[:], np.float64)
         self.last_stats = stats
         return us
+
+
+def _main(argv=None):
+    """Timing of one batch: python -m miccai2016_gb300.batched --side 128 --instances 64
+    Prints one JSON line with the batch's solves/s and the per-launch device
+    time of the batched flow and label sweeps (CUDA events)."""
+    import argparse
+    import json
+    import time
+
+    import torch
+
+    from . import phantom as P
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--side", type=int, default=128)
+    ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--iters", type=int, default=60)
+    ap.add_argument("--time-kernels", action="store_true")
+    a = ap.parse_args(argv)
+    shape = (a.side,) * 3
+    s = a.side / 128.0
+    noisy, truth, quats, ntw, fgw, bgw = P.maxflow_inputs(dict(shape=shape, tube_radius=6 * s, helix_radius=32 * s,
+                                                               pitch=40 * s, sigma=1.5, seed=0, weighting=0.05,
+                                                               decay=30.0))
+    grad2 = P.grad_mag_sq(noisy).astype(np.float32)
+    p = BatchedCut.CutParameters()
+    p.num_iter, p.update, p.error_bound = a.iters, 30, -1.0
+    bc = BatchedCut(p)
+    vol = bc.prepare_volume(noisy, quats, fgw, bgw, grad2=grad2)
+    ws = np.logspace(-2.5, 0.5, 25)
+    ds = np.logspace(-1, 3, 17)
+    insts = [dict(volume=0, weighting=ws[k % 25], decay=ds[k % 17], eigs=P.ATV_EIGS) for k in range(a.instances)]
+    bc.solve([vol], insts[:1])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bc.solve([vol], insts, time_kernels=a.time_kernels)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    st = bc.last_stats
+    n = int(np.prod(shape))
+    out = dict(side=a.side, instances=a.instances, iters=a.iters, wall_s=dt,
+               voxel_iterations_per_s=a.instances * a.iters * n / dt)
+    if a.time_kernels and st.p_launches:
+        pm = (st.p_ms + st.u_ms) / st.p_launches
+        # state bytes per instance and voxel-iteration: the flow sweep reads
+        # tmp 4 + hp 12 and writes hp 12, the label sweep reads hp 12 + pt 4 +
+        # u 4 and writes pt 4 + u 4 + tmp 4 = 60 B.  The volume's shared fields
+        # (read once per group of four) are not counted.
+        sb = 60.0
+        out.update(iteration_ms=pm, state_bytes=sb, state_gbs=sb * a.instances * n / (pm * 1e-3) / 1e9)
+        if st.u_launches:
+            out.update(flow_ms=st.p_ms / st.p_launches, label_ms=st.u_ms / st.u_launches)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    _main()

@@ -53,6 +53,9 @@ class CmfCutQAnisotropicGpu(TreePrintable):
         self.last_iterations = None
         self.last_residuals = None
         self._ws = None
+        # how an iteration is launched (N.PATH_DEFAULT, PATH_TWO_SWEEPS or
+        # PATH_FUSED); the paths give the same result within float rounding
+        self.iteration_path = N.PATH_DEFAULT
 
     # -- reference: execute() with its exception-forwarding wrapper (:143-196)
     def execute(self, img, quats, eigs, alpha, cs, ct, labels=None, scaling=None, verbose=True):
@@ -124,11 +127,13 @@ class CmfCutQAnisotropicGpu(TreePrintable):
         resid = (ctypes.c_double * cap)()
         iters = ctypes.c_int32(0)
         nres = ctypes.c_int32(0)
-        st = L.m16_maxflow_solve(N.ptr(d_img), N.ptr(d_q), sqc, N.ptr(sqp), N.ptr(d_alpha), alpha_scalar,
-                                 N.ptr(d_cs), N.ptr(d_ct), N.ptr(d_lab), shape[0], shape[1], shape[2],
-                                 ctypes.byref(cp), N.ptr(u), ctypes.byref(iters), resid, cap,
-                                 ctypes.byref(nres), N.ptr(self._ws), self._ws.numel(), N.stream_ptr())
-        N.check("m16_maxflow_solve", st)
+        stats = N.SolveStats(0, 0, 0, 0, 0.0, 0.0, int(self.iteration_path), 0)
+        st = L.m16_maxflow_solve_ex(N.ptr(d_img), N.ptr(d_q), sqc, N.ptr(sqp), N.ptr(d_alpha), alpha_scalar,
+                                    N.ptr(d_cs), N.ptr(d_ct), N.ptr(d_lab), shape[0], shape[1], shape[2],
+                                    ctypes.byref(cp), N.ptr(u), ctypes.byref(iters), resid, cap,
+                                    ctypes.byref(nres), N.ptr(self._ws), self._ws.numel(), N.stream_ptr(),
+                                    ctypes.byref(stats))
+        N.check("m16_maxflow_solve_ex", st)
         self.last_iterations = int(iters.value)
         self.last_residuals = np.array(resid[:min(nres.value, cap)], dtype=np.float64)
         if verbose:

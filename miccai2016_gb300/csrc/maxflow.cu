@@ -27,6 +27,7 @@
 
 #include "common.cuh"
 #include "sweeps.cuh"
+#include "fused.cuh"
 
 namespace m16 {
 namespace {
@@ -46,6 +47,7 @@ struct MfArgs {
     float sq0, sq1, sq2, isq0, isq1, isq2;
     float alpha_scalar;
     float *hp0, *hp1, *hp2, *tmp, *pt, *u;
+    float *hpB0, *hpB1, *hpB2, *tmpB;   // second ping-pong set of the fused iteration
     const float4 *q4;
     const float *alpha, *sqeigs, *cs, *ct;
     const uint8_t *labels;
@@ -119,6 +121,10 @@ __global__ void mf_init_kernel(MfArgs a, const float *__restrict__ img, const fl
 #ifndef M16_MF_MINB
 #define M16_MF_MINB 1
 #endif
+// resident blocks per SM the fused kernel is compiled for (3 caps it at 64 registers)
+#ifndef M16_MF_FUSED_MINB
+#define M16_MF_FUSED_MINB 3
+#endif
 constexpr int kZB = kMfZB;
 
 __device__ __forceinline__ FlowView flow_view(const MfArgs &a)
@@ -172,6 +178,62 @@ __global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_u_kernel(MfA
     }
 }
 
+// ---- the fused iteration (fused.cuh): P and U in one launch ---------------------
+// parity 0 reads (hp, tmp) and writes (hpB, tmpB); parity 1 the other way round.
+template <bool POINTWISE, bool ALPHA_ARR, bool SUPERVISED, bool CHECK>
+__global__ void __launch_bounds__(kFX * kFY, M16_MF_FUSED_MINB) mf_fused_kernel(MfArgs a, int parity)
+{
+    __shared__ float sm[2][2][kFY][kFX];
+    __shared__ float vals[kFX * kFY];
+    if (__ldcg(&a.ctrl->stopped)) return;
+    FusedView f;
+    f.d0 = a.d0; f.d1 = a.d1; f.d2 = a.d2;
+    f.ss0 = a.ss0; f.ss1 = a.ss1; f.ss2 = a.ss2; f.rcc = a.rcc; f.rs0 = a.rs0; f.rs1 = a.rs1; f.rs2 = a.rs2;
+    f.sq0 = a.sq0; f.sq1 = a.sq1; f.sq2 = a.sq2; f.isq0 = a.isq0; f.isq1 = a.isq1; f.isq2 = a.isq2;
+    f.alpha_scalar = a.alpha_scalar; f.alpha = a.alpha; f.grad2 = nullptr; f.w = 0.f; f.neg_inv_decay2 = 0.f;
+    f.exp_alpha = 0;
+    f.sqeigs = a.sqeigs; f.q4 = a.q4;
+    if (parity == 0) {
+        f.tmp_in = a.tmp; f.hp0_in = a.hp0; f.hp1_in = a.hp1; f.hp2_in = a.hp2;
+        f.tmp_out = a.tmpB; f.hp0_out = a.hpB0; f.hp1_out = a.hpB1; f.hp2_out = a.hpB2;
+    } else {
+        f.tmp_in = a.tmpB; f.hp0_in = a.hpB0; f.hp1_in = a.hpB1; f.hp2_in = a.hpB2;
+        f.tmp_out = a.tmp; f.hp0_out = a.hp0; f.hp1_out = a.hp1; f.hp2_out = a.hp2;
+    }
+    f.cs = a.cs; f.ct = a.ct; f.labels = a.labels; f.pt = a.pt; f.u = a.u;
+    const int z0 = blockIdx.z * a.zc;
+    const float acc = fused_tile<POINTWISE, ALPHA_ARR ? kAlphaArray : kAlphaScalar, SUPERVISED>(
+        f, blockIdx.x, blockIdx.y, z0, min(z0 + a.zc, a.d0), sm);
+    if (CHECK) {
+        const float s = fused_block_sum(acc, vals);
+        if (threadIdx.x == 0 && threadIdx.y == 0)
+            a.partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
+    }
+}
+
+template <bool CHECK>
+void launch_fused(bool pointwise, bool alpha_arr, bool sup, dim3 grid, cudaStream_t st, const MfArgs &a, int parity)
+{
+    const dim3 block(kFX, kFY, 1);
+    if (pointwise) {
+        if (alpha_arr) {
+            if (sup) mf_fused_kernel<true, true, true, CHECK><<<grid, block, 0, st>>>(a, parity);
+            else mf_fused_kernel<true, true, false, CHECK><<<grid, block, 0, st>>>(a, parity);
+        } else {
+            if (sup) mf_fused_kernel<true, false, true, CHECK><<<grid, block, 0, st>>>(a, parity);
+            else mf_fused_kernel<true, false, false, CHECK><<<grid, block, 0, st>>>(a, parity);
+        }
+    } else {
+        if (alpha_arr) {
+            if (sup) mf_fused_kernel<false, true, true, CHECK><<<grid, block, 0, st>>>(a, parity);
+            else mf_fused_kernel<false, true, false, CHECK><<<grid, block, 0, st>>>(a, parity);
+        } else {
+            if (sup) mf_fused_kernel<false, false, true, CHECK><<<grid, block, 0, st>>>(a, parity);
+            else mf_fused_kernel<false, false, false, CHECK><<<grid, block, 0, st>>>(a, parity);
+        }
+    }
+}
+
 // residual = sum(partials) / (N * rcc); stop on NaN or below the bound
 // (continuous_cut_anisotropic_gpu.py:321-337)
 __global__ void mf_check_kernel(const float *__restrict__ part, int nparts, double inv_norm, double bound,
@@ -201,7 +263,7 @@ __global__ void mf_check_kernel(const float *__restrict__ part, int nparts, doub
 // ---- host side --------------------------------------------------------------
 
 struct MfLayout {
-    size_t hp0, hp1, hp2, pt, tmp, q4, partials, maxpart, ctrl, resid, total;
+    size_t hp0, hp1, hp2, pt, tmp, hpB0, hpB1, hpB2, tmpB, q4, partials, maxpart, ctrl, resid, total;
     int nparts, resid_cap;
 };
 
@@ -219,7 +281,8 @@ inline int choose_zc(int d0, int d1, int d2)
     return (int)zc;
 }
 
-inline MfLayout mf_layout(int d0, int d1, int d2, int num_iter, int update)
+// fused: with the second ping-pong set of hp and tmp the fused iteration needs
+inline MfLayout mf_layout(int d0, int d1, int d2, int num_iter, int update, bool fused)
 {
     MfLayout L;
     const int64_t n = (int64_t)d0 * d1 * d2;
@@ -229,7 +292,10 @@ inline MfLayout mf_layout(int d0, int d1, int d2, int num_iter, int update)
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
     L.hp0 = take(n * 4); L.hp1 = take(n * 4); L.hp2 = take(n * 4);
-    L.pt = take(n * 4); L.tmp = take(n * 4); L.q4 = take(n * 16);
+    L.pt = take(n * 4); L.tmp = take(n * 4);
+    L.hpB0 = L.hpB1 = L.hpB2 = L.tmpB = 0;
+    if (fused) { L.hpB0 = take(n * 4); L.hpB1 = take(n * 4); L.hpB2 = take(n * 4); L.tmpB = take(n * 4); }
+    L.q4 = take(n * 16);
     L.partials = take((size_t)L.nparts * 4);
     L.maxpart = take(kMaxBlocks * 4);
     L.ctrl = take(sizeof(MfCtrl));
@@ -248,7 +314,7 @@ using namespace m16;
 extern "C" size_t m16_maxflow_workspace_bytes(int32_t d0, int32_t d1, int32_t d2, const m16_cut_params *params)
 {
     if (d0 < 1 || d1 < 1 || d2 < 1 || !params) return 0;
-    return mf_layout(d0, d1, d2, params->num_iter, params->update).total;
+    return mf_layout(d0, d1, d2, params->num_iter, params->update, true).total;
 }
 
 extern "C" int m16_maxflow_solve(const float *img, const float *quat3, const double *sqevals3,
@@ -282,13 +348,14 @@ struct EventPool {
 };
 }  // namespace
 
-extern "C" int m16_maxflow_solve_ex(const float *img, const float *quat3, const double *sqevals3,
-                                    const float *sqeigs, const float *alpha, float alpha_scalar,
-                                    const float *cs, const float *ct, const uint8_t *labels,
-                                    int32_t d0, int32_t d1, int32_t d2, const m16_cut_params *params,
-                                    float *u, int32_t *iterations, double *residuals, int32_t residuals_cap,
-                                    int32_t *n_residuals, void *workspace, size_t workspace_bytes, void *stream,
-                                    m16_solve_stats *stats)
+// The solve; fused selects the one-launch iteration (fused.cuh, ping-pong
+// workspace) over the two sweeps.
+static int maxflow_solve_impl(const float *img, const float *quat3, const double *sqevals3, const float *sqeigs,
+                              const float *alpha, float alpha_scalar, const float *cs, const float *ct,
+                              const uint8_t *labels, int32_t d0, int32_t d1, int32_t d2,
+                              const m16_cut_params *params, float *u, int32_t *iterations, double *residuals,
+                              int32_t residuals_cap, int32_t *n_residuals, void *workspace, size_t workspace_bytes,
+                              void *stream, m16_solve_stats *stats, bool fused)
 {
     if (d0 < 1 || d1 < 1 || d2 < 1) return M16_ERR_BAD_SHAPE;
     if ((int64_t)d0 * d1 * d2 > ((int64_t)1 << 34)) return M16_ERR_BAD_SHAPE;
@@ -301,7 +368,7 @@ extern "C" int m16_maxflow_solve_ex(const float *img, const float *quat3, const 
     if (sqevals3)
         for (int k = 0; k < 3; ++k)
             if (!finite_pos(sqevals3[k])) return M16_ERR_BAD_ARG;
-    const MfLayout L = mf_layout(d0, d1, d2, params->num_iter, params->update);
+    const MfLayout L = mf_layout(d0, d1, d2, params->num_iter, params->update, fused);
     if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;
     cudaStream_t st = (cudaStream_t)stream;
     char *ws = (char *)workspace;
@@ -324,6 +391,10 @@ extern "C" int m16_maxflow_solve_ex(const float *img, const float *quat3, const 
     a.alpha_scalar = alpha_scalar;
     a.hp0 = (float *)(ws + L.hp0); a.hp1 = (float *)(ws + L.hp1); a.hp2 = (float *)(ws + L.hp2);
     a.pt = (float *)(ws + L.pt); a.tmp = (float *)(ws + L.tmp); a.u = u;
+    a.hpB0 = fused ? (float *)(ws + L.hpB0) : nullptr;
+    a.hpB1 = fused ? (float *)(ws + L.hpB1) : nullptr;
+    a.hpB2 = fused ? (float *)(ws + L.hpB2) : nullptr;
+    a.tmpB = fused ? (float *)(ws + L.tmpB) : nullptr;
     a.q4 = (const float4 *)(ws + L.q4);
     a.alpha = alpha; a.sqeigs = sqeigs; a.cs = cs; a.ct = ct; a.labels = labels;
     a.partials = (float *)(ws + L.partials);
@@ -362,6 +433,22 @@ extern "C" int m16_maxflow_solve_ex(const float *img, const float *quat3, const 
         const int first = it;
         for (; it < end; ++it) {
             if (timing) cudaEventRecord(pool->ev[3 * (it - first)], st);
+            if (fused) {
+                const bool check = (it % update) == 0;
+                if (check) launch_fused<true>(pointwise, alpha_arr, sup, grid, st, a, it & 1);
+                else launch_fused<false>(pointwise, alpha_arr, sup, grid, st, a, it & 1);
+                if (timing) {
+                    cudaEventRecord(pool->ev[3 * (it - first) + 1], st);
+                    cudaEventRecord(pool->ev[3 * (it - first) + 2], st);
+                }
+                if (check) {
+                    mf_check_kernel<<<1, 256, 0, st>>>(a.partials, L.nparts, inv_norm, params->error_bound, it,
+                                                       it / update, L.resid_cap, a.ctrl, resid);
+                    ++launches;
+                }
+                ++launches;
+                continue;
+            }
             if (pointwise) {
                 if (alpha_arr) mf_update_p_kernel<true, true><<<grid, block, 0, st>>>(a);
                 else mf_update_p_kernel<true, false><<<grid, block, 0, st>>>(a);
@@ -406,7 +493,7 @@ extern "C" int m16_maxflow_solve_ex(const float *img, const float *quat3, const 
     if (stats) {
         stats->launches = launches;
         stats->p_launches = timing ? p_launches : std::min(it, hctrl.stopped ? hctrl.iterations : it);
-        stats->u_launches = stats->p_launches;
+        stats->u_launches = fused ? 0 : stats->p_launches;
         stats->p_ms = p_ms;
         stats->u_ms = u_ms;
     }
@@ -422,6 +509,21 @@ extern "C" int m16_maxflow_solve_ex(const float *img, const float *quat3, const 
         }
     }
     return M16_OK;
+}
+
+extern "C" int m16_maxflow_solve_ex(const float *img, const float *quat3, const double *sqevals3,
+                                    const float *sqeigs, const float *alpha, float alpha_scalar,
+                                    const float *cs, const float *ct, const uint8_t *labels,
+                                    int32_t d0, int32_t d1, int32_t d2, const m16_cut_params *params,
+                                    float *u, int32_t *iterations, double *residuals, int32_t residuals_cap,
+                                    int32_t *n_residuals, void *workspace, size_t workspace_bytes, void *stream,
+                                    m16_solve_stats *stats)
+{
+    if (stats && (stats->path < M16_PATH_DEFAULT || stats->path > M16_PATH_FUSED)) return M16_ERR_BAD_ARG;
+    const bool fused = stats && stats->path == M16_PATH_FUSED;
+    return maxflow_solve_impl(img, quat3, sqevals3, sqeigs, alpha, alpha_scalar, cs, ct, labels, d0, d1, d2, params,
+                              u, iterations, residuals, residuals_cap, n_residuals, workspace, workspace_bytes,
+                              stream, stats, fused);
 }
 
 // ---- fixed-footprint variant: no allocation by anyone --------------------------
@@ -487,7 +589,7 @@ extern "C" int m16_maxflow_solve_static(const float *img, const float *quat3, co
     if (params->update < 1 || params->num_iter < 0) return M16_ERR_BAD_ARG;
     if ((int64_t)d0 * d1 * d2 > kStaticMaxVoxels) return M16_ERR_TOO_LARGE;
     if (params->num_iter / params->update + 2 > kStaticMaxChecks) return M16_ERR_TOO_LARGE;
-    const MfLayout L = mf_layout(d0, d1, d2, params->num_iter, params->update);
+    const MfLayout L = mf_layout(d0, d1, d2, params->num_iter, params->update, false);
     if (L.total > kStaticBytes) return M16_ERR_TOO_LARGE;
     void *scratch = nullptr;
     const int st = static_scratch_on_current_device(&scratch);
@@ -495,7 +597,8 @@ extern "C" int m16_maxflow_solve_static(const float *img, const float *quat3, co
     // The solve's initialisation kernels write every scratch word before it is
     // read (flow state, control word, partial sums), so nothing of the previous
     // call's contents leaks into this one.
-    return m16_maxflow_solve_ex(img, quat3, sqevals3, sqeigs, alpha, alpha_scalar, cs, ct, labels, d0, d1, d2,
-                                params, u, iterations, residuals, residuals_cap, n_residuals, scratch, kStaticBytes,
-                                stream, nullptr);
+    // the two-sweep iteration: its workspace fits the fixed array
+    return maxflow_solve_impl(img, quat3, sqevals3, sqeigs, alpha, alpha_scalar, cs, ct, labels, d0, d1, d2, params,
+                              u, iterations, residuals, residuals_cap, n_residuals, scratch, kStaticBytes, stream,
+                              nullptr, false);
 }

@@ -18,7 +18,9 @@ namespace m16 {
 constexpr int kMfZB = M16_MF_ZB;   // z-slices whose loads are issued together
 
 // where the projection radius alpha comes from
-enum AlphaMode { kAlphaScalar = 0, kAlphaArray = 1, kAlphaFromGrad2 = 2 };
+// kAlphaSource: read `alpha` and, when exp_alpha is set, use w * exp(neg_inv_decay2 * value)
+// (one code path for instances with an alpha field and with (weighting, decay))
+enum AlphaMode { kAlphaScalar = 0, kAlphaArray = 1, kAlphaFromGrad2 = 2, kAlphaSource = 3 };
 
 // Everything one instance's flow sweep reads and writes.
 struct FlowView {

@@ -76,3 +76,16 @@ def test_solve_rejects_bad_arguments_before_touching_the_gpu(lib):
     st = lib.m16_maxflow_solve(fake, fake, None, None, None, 0.1, fake, fake, None, 4, 4, 4, ctypes.byref(p), fake,
                                ctypes.byref(it), None, 0, None, fake, 1 << 20, None)
     assert st == N.M16_ERR_BAD_ARG
+
+
+def test_solve_ex_rejects_an_unknown_iteration_path(lib):
+    from miccai2016_gb300 import _native as N
+    p = N.CutParams(0.2, 0.11, 1e-4, 100, 10, (ctypes.c_double * 3)(1, 1, 1))
+    it = ctypes.c_int32(0)
+    sq = (ctypes.c_double * 3)(1, 1, 1)
+    fake = ctypes.c_void_p(256)
+    for path in (-1, 3):
+        s = N.SolveStats(0, 0, 0, 0, 0.0, 0.0, path, 0)
+        st = lib.m16_maxflow_solve_ex(fake, fake, sq, None, None, 0.1, fake, fake, None, 4, 4, 4, ctypes.byref(p),
+                                      fake, ctypes.byref(it), None, 0, None, fake, 1 << 20, None, ctypes.byref(s))
+        assert st == N.M16_ERR_BAD_ARG

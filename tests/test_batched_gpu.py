@@ -88,3 +88,21 @@ def test_grid_search_shape_of_the_reference():
     for k in (0, 200, 424):
         u, _ = _plain(vols[0], insts[k], 60, 30, -1.0)
         assert np.max(np.abs(us[k] - u)) <= U_TOL
+
+
+def test_groups_of_four_with_padding_and_mixed_eigenvalues():
+    """Instances are grouped four to a group by (volume, eigenvalues, alpha
+    kind), interleaved lane by lane; 7 instances of two eigenvalue sets give
+    partly filled groups whose padding lanes must not disturb the real ones,
+    and an instance alone in its group must match too."""
+    vols = [_volume(5, (20, 18, 40))]
+    insts = []
+    for k in range(7):
+        e = ATV if k % 3 else TV
+        insts.append(dict(volume=0, weighting=0.02 * (k + 1), decay=0.5 * (k + 1), eigs=e))
+    insts.append(dict(volume=0, weighting=0.1, decay=2.0, eigs=(1.0, 0.3, 0.2)))
+    us, its = _batch(vols, insts, 90, 30, -1.0)
+    for k, inst in enumerate(insts):
+        u, it = _plain(vols[0], inst, 90, 30, -1.0)
+        assert its[k] == it == 90
+        assert np.max(np.abs(us[k] - u)) <= U_TOL, k

@@ -34,18 +34,28 @@ def _cutter(num_iter, update, error_bound, cc=0.2, steps=0.11):
     return CmfCutQAnisotropicGpu(p)
 
 
-def _run_gpu(inp, kw):
+PATHS = ["two_sweeps", "fused"]
+
+
+def _path_code(path):
+    from miccai2016_gb300 import _native as N
+    return {"default": N.PATH_DEFAULT, "two_sweeps": N.PATH_TWO_SWEEPS, "fused": N.PATH_FUSED}[path]
+
+
+def _run_gpu(inp, kw, path="default"):
     c = _cutter(kw["num_iter"], kw["update"], kw["error_bound"])
+    c.iteration_path = _path_code(path)
     u = c.execute(inp["img"], inp["quats"], inp["eigs"], inp["alpha"], inp["cs"], inp["ct"],
                   labels=inp["labels"], scaling=inp["scaling"], verbose=False)
     return u, c.last_iterations, c.last_residuals
 
 
+@pytest.mark.parametrize("path", PATHS)
 @pytest.mark.parametrize("name", I.MAXFLOW_CASES)
-def test_golden_fixtures(name):
+def test_golden_fixtures(name, path):
     inp, kw = I.maxflow_case(name)
     g = np.load(os.path.join(HERE, "golden", name + ".npz"))
-    u, iters, resid = _run_gpu(inp, kw)
+    u, iters, resid = _run_gpu(inp, kw, path)
     assert u.dtype == np.float32 and u.shape == g["u"].shape
     if kw["error_bound"] < 0:
         assert iters == int(g["iterations"])
@@ -60,7 +70,8 @@ def test_golden_fixtures(name):
 @pytest.mark.parametrize("shape", [(1, 1, 1), (1, 6, 1), (5, 7, 9), (3, 1, 70), (33, 9, 40), (70, 3, 5)])
 @pytest.mark.parametrize("supervised", [False, True])
 @pytest.mark.parametrize("pointwise", [False, True])
-def test_random_variants_match_oracle(shape, supervised, pointwise):
+@pytest.mark.parametrize("path", PATHS)
+def test_random_variants_match_oracle(shape, supervised, pointwise, path):
     rng = np.random.RandomState(abs(hash((shape, supervised, pointwise))) % 2 ** 31)
     img = rng.normal(0.5, 0.5, shape).astype(np.float32)
     q = I.random_squeezed(rng, shape)
@@ -72,7 +83,7 @@ def test_random_variants_match_oracle(shape, supervised, pointwise):
     sc = (1.5, 0.7, 1.2) if (shape[0] % 2) else (1, 1, 1)
     inp = dict(img=img, quats=q, eigs=eigs, alpha=alpha, cs=cs, ct=ct, labels=lab, scaling=sc)
     kw = dict(num_iter=100, update=10, error_bound=-1.0)
-    u, iters, _ = _run_gpu(inp, kw)
+    u, iters, _ = _run_gpu(inp, kw, path)
     ru, riters, _ = O.maxflow_solve(img, q, eigs, alpha, cs, ct, labels=lab, scaling=sc, **kw)
     assert iters == riters == 100
     assert np.max(np.abs(u - ru)) <= U_TOL
@@ -83,14 +94,16 @@ def _helix_inputs(cfg):
     return P.maxflow_inputs(cfg)
 
 
+@pytest.mark.parametrize("path", PATHS)
 @pytest.mark.parametrize("eigs_name", ["atv", "tv"])
-def test_helix_64_fixed_iterations_parity(eigs_name):
+def test_helix_64_fixed_iterations_parity(eigs_name, path):
     """The plain 64^3 configuration: 300 fixed iterations, ATV and TV."""
     from miccai2016_gb300 import phantom as P
     cfg = P.CONFIG_PLAIN_64
     eigs = P.ATV_EIGS if eigs_name == "atv" else P.TV_EIGS
     noisy, truth, quats, ntw, fgw, bgw = _helix_inputs(cfg)
     c = _cutter(cfg["num_iter"], 30, -1.0)
+    c.iteration_path = _path_code(path)
     u = c.execute(noisy, quats, eigs, ntw, fgw, bgw, labels=None, scaling=(1, 1, 1), verbose=False)
     ru, riters, _ = O.maxflow_solve(noisy, quats, eigs, ntw, fgw, bgw, num_iter=cfg["num_iter"], update=30,
                                     error_bound=-1.0)
@@ -102,12 +115,14 @@ def test_helix_64_fixed_iterations_parity(eigs_name):
         assert P.fast_dice(u, truth) > 0.3
 
 
-def test_residual_stop_matches_oracle():
+@pytest.mark.parametrize("path", PATHS)
+def test_residual_stop_matches_oracle(path):
     from miccai2016_gb300 import phantom as P
     cfg = P.CONFIG_PLAIN_64
     noisy, truth, quats, ntw, fgw, bgw = _helix_inputs(cfg)
     kw = dict(num_iter=3000, update=30, error_bound=1e-3)
     c = _cutter(**kw)
+    c.iteration_path = _path_code(path)
     u = c.execute(noisy, quats, P.ATV_EIGS, ntw, fgw, bgw, verbose=False)
     ru, riters, rres = O.maxflow_solve(noisy, quats, P.ATV_EIGS, ntw, fgw, bgw, **kw)
     assert riters < kw["num_iter"]
@@ -150,3 +165,14 @@ def test_scalar_and_array_alpha_agree():
     ua, _, _ = _run_gpu(a, kw)
     ub, _, _ = _run_gpu(b, kw)
     assert np.array_equal(ua, ub)
+
+
+def test_two_sweeps_and_fused_paths_agree():
+    """The two iteration paths do the same per-voxel arithmetic; they may
+    differ only by float contraction choices, far inside the oracle tolerance."""
+    inp, kw = I.maxflow_case("mf_const_unsup")
+    u2, i2, r2 = _run_gpu(inp, kw, "two_sweeps")
+    uf, i_f, rf = _run_gpu(inp, kw, "fused")
+    assert i2 == i_f
+    assert np.max(np.abs(u2 - uf)) <= 1e-5
+    np.testing.assert_allclose(r2, rf, rtol=1e-4)

@@ -85,7 +85,10 @@ def test_static_matches_workspace_entry_point_on_two_calls_in_a_row():
         u_w, it_w, r_w = _solve(N, L, False, case)
         assert it_s == it_w == 60
         assert np.max(np.abs(u_s - u_w)) <= U_TOL
-        np.testing.assert_allclose(r_s, r_w, rtol=1e-6)
+        # the static entry point runs the two-sweep iteration, the workspace
+        # one the fused kernel: the same per-voxel arithmetic, but the float
+        # sums of |err| are taken in a different order (columns vs tiles)
+        np.testing.assert_allclose(r_s, r_w, rtol=1e-4)
 
 
 def test_static_rejects_requests_beyond_its_scratch():
