@@ -364,8 +364,11 @@ def run_ours(args, cfg):
                              "sample": sample},
             "clocks": clocks, "dice_fast": dice,
             "voxel_iterations_per_s": value * n * cfg["num_iter"]}
-    if cfg["name"] == "plain256":   # the default workload also reports the batched grid search
+    if cfg["name"] == "plain256":   # the default workload also reports the batched grid search and serving
         line["batched"] = run_batched_grid()
+        if args.served_requests > 0:
+            from miccai2016_gb300.serving import served_vs_plain
+            line["served"] = served_vs_plain(n_requests=args.served_requests, rate=50.0, pool=8)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -459,6 +462,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain256")
     ap.add_argument("--ref-iters", type=int, default=3, help="iterations per CPU-baseline sample")
+    ap.add_argument("--served-requests", type=int, default=96,
+                    help="requests of the serving comparison (0 skips it)")
     args = ap.parse_args()
     cfg = _workload(args.workload)
     if args.impl == "reference":

@@ -192,6 +192,72 @@ int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const m16_batch_
                     const m16_cut_params *params, int32_t *iterations, double *residuals, void *workspace,
                     size_t workspace_bytes, void *stream, m16_solve_stats *stats);
 
+/* ---- serving: continuous batching of max-flow requests ----------------------
+ * No reference interface: the reference solves one CmfCutQAnisotropicGpu at a
+ * time.  A server owns one caller workspace; requests (each its own volume)
+ * are admitted while the workspace has room, their inputs are uploaded on a
+ * copy stream, and every m16_server_step advances all resident requests by
+ * params->update iterations (one residual check each, at the request's own
+ * iterations 0, update, 2 update, ...), so a request's iterations, residuals
+ * and u are the same as those of m16_maxflow_solve on its inputs alone.  A
+ * request retires at the residual bound (or NaN) or at params->num_iter; its
+ * u is then copied to the request's host buffer and the memory is reused. */
+typedef struct m16_server m16_server;
+
+typedef struct m16_serve_request {
+    int32_t d0, d1, d2, reserved;
+    const float *img;     /* host, N: u starts as img / (max(img) + FLT_MIN) */
+    const float *quat3;   /* host, N x 3 squeezed quaternions */
+    const float *grad2;   /* host, N: |grad img|^2 for alpha = weighting * exp(-grad2 / decay^2) ... */
+    const float *alpha;   /* ... or host, N per-voxel alpha (then grad2 is ignored) */
+    const float *cs;      /* host, N source capacities */
+    const float *ct;      /* host, N sink capacities */
+    double scaling[3];
+    double weighting, decay;
+    double sqevals[3];    /* square roots of the constant eigenvalues */
+    float *u;             /* host, N output, written when the request retires */
+    int64_t tag;          /* caller's identifier, returned by m16_server_poll */
+} m16_serve_request;
+
+typedef struct m16_server_info {
+    int32_t resident;     /* admitted and iterating */
+    int32_t draining;     /* retired, u on its way to the host */
+    int32_t free_slots;
+    int32_t reserved;
+    int64_t free_bytes;   /* workspace not held by requests */
+    int64_t largest_free; /* largest request allocation that fits now */
+    int64_t steps;        /* m16_server_step calls that ran iterations */
+} m16_server_info;
+
+/* Workspace bytes a request of d0 x d1 x d2 voxels holds while resident. */
+size_t m16_server_request_bytes(int32_t d0, int32_t d1, int32_t d2, int32_t has_alpha);
+
+/* Workspace bytes the server keeps for its tables (the rest holds requests). */
+size_t m16_server_table_bytes(int32_t max_slots, int32_t max_work_items);
+
+/* params->num_iter must be a multiple of params->update.  workspace: device,
+ * 256-byte aligned; stream: the compute stream (requests upload and download
+ * on a stream of the server's own). */
+int m16_server_create(const m16_cut_params *params, int32_t max_slots, int32_t max_work_items, void *workspace,
+                      size_t workspace_bytes, void *stream, m16_server **out);
+
+/* *admitted = 1 when the request got a slot and memory, else 0 (try again
+ * after requests retire).  The host buffers must stay valid until the
+ * request has been returned by m16_server_poll. */
+int m16_server_admit(m16_server *s, const m16_serve_request *req, int32_t *admitted);
+
+/* params->update iterations of every resident request, then retirement. */
+int m16_server_step(m16_server *s);
+
+/* Requests whose u has reached the host since the last call: tags,
+ * iteration counts and last residuals (host arrays of cap entries). */
+int m16_server_poll(m16_server *s, int64_t *tags, int32_t *iterations, double *residuals, int32_t cap, int32_t *n);
+
+int m16_server_get_info(const m16_server *s, m16_server_info *info);
+
+/* Waits for the server's work and frees its host resources. */
+int m16_server_destroy(m16_server *s);
+
 /* ---- gradient vector flow --------------------------------------------------
  * Workspace bytes of m16_gvf_run; has_response says whether a response field
  * will be passed, mags_cap bounds the convergence log (maxiter / update + 1). */

@@ -71,6 +71,19 @@ class BatchInstance(ctypes.Structure):
                 ("sqevals", _f64 * 3), ("u", _vp)]
 
 
+class ServeRequest(ctypes.Structure):
+    """m16_serve_request (include/miccai2016_gb300.h)."""
+    _fields_ = [("d0", _i32), ("d1", _i32), ("d2", _i32), ("reserved", _i32), ("img", _vp), ("quat3", _vp),
+                ("grad2", _vp), ("alpha", _vp), ("cs", _vp), ("ct", _vp), ("scaling", _f64 * 3),
+                ("weighting", _f64), ("decay", _f64), ("sqevals", _f64 * 3), ("u", _vp), ("tag", _i64)]
+
+
+class ServerInfo(ctypes.Structure):
+    """m16_server_info (include/miccai2016_gb300.h)."""
+    _fields_ = [("resident", _i32), ("draining", _i32), ("free_slots", _i32), ("reserved", _i32),
+                ("free_bytes", _i64), ("largest_free", _i64), ("steps", _i64)]
+
+
 def _declare(L):
     L.m16_status_string.restype = ctypes.c_char_p
     L.m16_status_string.argtypes = [ctypes.c_int]
@@ -106,6 +119,22 @@ def _declare(L):
     L.m16_batch_solve.restype = ctypes.c_int
     L.m16_batch_solve.argtypes = [ctypes.POINTER(BatchVolume), _i32, ctypes.POINTER(BatchInstance), _i32,
                                   ctypes.POINTER(CutParams), _vp, _vp, _vp, _sz, _vp, ctypes.POINTER(SolveStats)]
+    L.m16_server_request_bytes.restype = _sz
+    L.m16_server_request_bytes.argtypes = [_i32, _i32, _i32, _i32]
+    L.m16_server_table_bytes.restype = _sz
+    L.m16_server_table_bytes.argtypes = [_i32, _i32]
+    L.m16_server_create.restype = ctypes.c_int
+    L.m16_server_create.argtypes = [ctypes.POINTER(CutParams), _i32, _i32, _vp, _sz, _vp, ctypes.POINTER(_vp)]
+    L.m16_server_admit.restype = ctypes.c_int
+    L.m16_server_admit.argtypes = [_vp, ctypes.POINTER(ServeRequest), ctypes.POINTER(_i32)]
+    L.m16_server_step.restype = ctypes.c_int
+    L.m16_server_step.argtypes = [_vp]
+    L.m16_server_poll.restype = ctypes.c_int
+    L.m16_server_poll.argtypes = [_vp, _vp, _vp, _vp, _i32, ctypes.POINTER(_i32)]
+    L.m16_server_get_info.restype = ctypes.c_int
+    L.m16_server_get_info.argtypes = [_vp, ctypes.POINTER(ServerInfo)]
+    L.m16_server_destroy.restype = ctypes.c_int
+    L.m16_server_destroy.argtypes = [_vp]
     L.m16_gvf_workspace_bytes.restype = _sz
     L.m16_gvf_workspace_bytes.argtypes = [_i32, _i32, _i32, _i32, _i32]
     L.m16_gvf_run.restype = ctypes.c_int

@@ -1,31 +1,6 @@
-// batched.cu -- many ATV max-flow solves in one launch per sweep.
-//
-// The reference runs its (weighting, decay) grid search as one
-// CmfCutQAnisotropicGpu.execute() per grid point and cut type
-// (src/phantom_experiment.py:350-368), each with three launches per iteration
-// and a blocking residual read every `update` iterations.  Here a batch of
-// instances -- any mix of volumes, weightings, decays and eigenvalue sets --
-// advances together: every flow (P) and label (U) launch covers all active
-// instances, the residual check of every instance is one block of one launch,
-// and an instance stops on its own at its threshold.
-//
-// Layout.  Instances of one volume with the same eigenvalues (and the same
-// kind of alpha) form groups of kLanes = 4; a group's state is interleaved,
-// one float4 per voxel and field (lane = instance), so one 16-byte load or
-// store serves four solves and a warp moves 512 contiguous bytes per field.
-// The volume's quaternions, |grad I|^2 and capacities are read once per voxel
-// for the whole group and the rotation is built once.  The projection radius
-// of a lane is its alpha field (gathered into an interleaved field at set-up)
-// or w * exp(-|grad I|^2 / decay^2) (phantom_experiment.py:359) computed in
-// the flow sweep, so per voxel and instance only the state streams from HBM:
-// flow reads tmp 4 + hp 12 and writes hp 12, labels read hp 12 + p_t 4 + u 4
-// and write p_t 4 + u 4 + tmp 4 -- 60 B per voxel-iteration.
-//
-// Stopping.  The check kernel sets a lane's bit in its group's stop mask; the
-// label sweep then keeps that lane's u (the solve's result) unchanged, blocks
-// of a group whose lanes have all stopped return at once, and the work list
-// drops finished groups.  At the end u is scattered out of the interleaved
-// field into each instance's output array.
+// batched.cu -- m16_batch_solve: a fixed batch of ATV max-flow instances
+// run to completion, every flow / label launch covering all active instances
+// (device side and layout in batch_kernels.cuh).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <float.h>
@@ -35,393 +10,79 @@
 #include <tuple>
 #include <vector>
 
-#include "common.cuh"
+#include "batch_kernels.cuh"
 
 namespace m16 {
 namespace {
-
-constexpr int kBX = 32, kBY = 8, kTile = kBX * kBY;
-constexpr int kLanes = 4;     // instances per group: one float4 per voxel and field
-constexpr int kFields = 6;    // hp0 hp1 hp2 pt tmp u (+ alpha for groups with alpha fields)
-constexpr unsigned kAllLanes = (1u << kLanes) - 1u;
-
-struct InstCtrl {
-    int stopped;
-    int iterations;
-    int n_checks;
-    int pad;
-    double resid;   // last checked residual
-};
-
-struct VolDev {
-    int d0, d1, d2, zc, tx, ty, tz, pad;
-    float rcc, rs0, rs1, rs2, ss0, ss1, ss2, denom;
-    const float4 *q4;
-    const float *grad2, *cs, *ct;
-    int64_t n;
-};
-
-struct GroupDev {
-    int vol, part_off, nparts, has_alpha;
-    float4 w, nid2;          // per lane: alpha = w * exp(nid2 * |grad I|^2), nid2 = -1 / decay^2
-    float sq0, sq1, sq2, isq0, isq1, isq2;
-    float4 *state;           // kFields (+1) slabs of `slab` float4
-    int64_t slab;
-};
-
-struct InstDev {
-    int group, lane;
-    float *u_out;
-    const float *alpha;
-};
-
-// z-slices per block: enough blocks for M16_BATCH_BLOCKS_PER_SM per SM over
-// the volume's groups (many short blocks keep the last wave short), at most 32
-#ifndef M16_BATCH_BLOCKS_PER_SM
-#define M16_BATCH_BLOCKS_PER_SM 16
-#endif
-#ifndef M16_BATCH_MINB
-#define M16_BATCH_MINB 3
-#endif
-inline int batch_zc(int d0, int d1, int d2, int ngroups_of_volume)
-{
-    const int64_t cols = div_up(d2, kBX) * div_up(d1, kBY);
-    int64_t zc = (int64_t)d0 * cols * std::max(ngroups_of_volume, 1) /
-                 ((int64_t)M16_BATCH_BLOCKS_PER_SM * kSMs);
-    zc = std::max<int64_t>(1, std::min<int64_t>(32, zc));
-    return (int)zc;
-}
-
-__device__ __forceinline__ float lane_of(const float4 &v, int l)
-{
-    return l == 0 ? v.x : (l == 1 ? v.y : (l == 2 ? v.z : v.w));
-}
-
-// ---- initialisation ---------------------------------------------------------
-
-__global__ void bt_max_kernel(const float *__restrict__ img, int64_t n, float *__restrict__ part)
-{
-    __shared__ float sm[32];
-    __shared__ int snan;
-    if (threadIdx.x == 0) snan = 0;
-    __syncthreads();
-    float m = -INFINITY;
-    int nan = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float v = img[i];
-        if (v != v) nan = 1; else m = fmaxf(m, v);
-    }
-    if (nan) snan = 1;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float r = sm[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = fmaxf(r, sm[w]);
-        part[blockIdx.x] = snan ? NAN : r;
-    }
-}
-
-__global__ void bt_denom_kernel(const float *__restrict__ part, int nparts, VolDev *vol)
-{
-    if (threadIdx.x != 0) return;
-    float m = -INFINITY;
-    bool nan = false;
-    for (int k = 0; k < nparts; ++k) {
-        const float v = part[k];
-        if (v != v) nan = true; else m = fmaxf(m, v);
-    }
-    vol->denom = (nan ? NAN : m) + FLT_MIN;   // np.max(img) + np.finfo(float32).tiny
-}
-
-__global__ void bt_expand_kernel(const float *__restrict__ quat3, float4 *__restrict__ q4, int64_t n)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        q4[i] = qexpand(quat3[3 * i], quat3[3 * i + 1], quat3[3 * i + 2]);
-}
-
-// every lane of a group: hp = 0, p_t = fmin(cs, ct), u = img / denom,
-// tmp = -u * rcc (continuous_cut_anisotropic_gpu.py:276-289)
-__global__ void bt_init_group_kernel(const float *__restrict__ img, const VolDev *vols, const GroupDev *groups, int g)
-{
-    const GroupDev &G = groups[g];
-    const VolDev &V = vols[G.vol];
-    const float denom = V.denom;
-    const int64_t S = G.slab;
-    float4 *st = G.state;
-    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < V.n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float ptv = fminf(V.cs[i], V.ct[i]);
-        const float ui = img[i] / denom;
-        const float ti = -(ui * V.rcc);
-        st[i] = zero;
-        st[S + i] = zero;
-        st[2 * S + i] = zero;
-        st[3 * S + i] = make_float4(ptv, ptv, ptv, ptv);
-        st[4 * S + i] = make_float4(ti, ti, ti, ti);
-        st[5 * S + i] = make_float4(ui, ui, ui, ui);
-    }
-}
-
-// interleave the lanes' alpha fields (absent lanes: 0)
-__global__ void bt_gather_alpha_kernel(const GroupDev *groups, int g, const float *a0, const float *a1,
-                                       const float *a2, const float *a3, int64_t n)
-{
-    const GroupDev &G = groups[g];
-    float4 *al = G.state + kFields * G.slab;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        al[i] = make_float4(a0 ? a0[i] : 0.f, a1 ? a1[i] : 0.f, a2 ? a2[i] : 0.f, a3 ? a3[i] : 0.f);
-}
-
-// u of one instance out of its group's interleaved field
-__global__ void bt_scatter_u_kernel(const GroupDev *groups, const InstDev *insts, int inst, int64_t n)
-{
-    const InstDev &I = insts[inst];
-    const GroupDev &G = groups[I.group];
-    const float *u4 = (const float *)(G.state + 5 * G.slab);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        I.u_out[i] = u4[4 * i + I.lane];
-}
-
-// ---- the sweeps ---------------------------------------------------------------
-// A work item is (group, tile); a block of 32 x 8 threads walks the tile's
-// z-chunk, one (y, x) column per thread, all four lanes of the group per voxel.
-
-__device__ __forceinline__ void decode_tile(const VolDev &V, int tile, int &bx, int &by, int &bz)
-{
-    bx = tile % V.tx;
-    by = (tile / V.tx) % V.ty;
-    bz = tile / (V.tx * V.ty);
-}
-
-// P (update_qp.cl:150-232) for the four lanes of a group
-template <bool ALPHA_ARR>
-__global__ void __launch_bounds__(kTile, M16_BATCH_MINB) bt_flow_kernel(const int2 *__restrict__ work,
-                                                                       const VolDev *vols, const GroupDev *groups,
-                                                                       const unsigned *__restrict__ gmask)
-{
-    const int2 wk = work[blockIdx.x];
-    if (__ldcg(gmask + wk.x) == kAllLanes) return;
-    const GroupDev &G = groups[wk.x];
-    const VolDev &V = vols[G.vol];
-    int bx, by, bz;
-    decode_tile(V, wk.y, bx, by, bz);
-    const int d0 = V.d0, d1 = V.d1, d2 = V.d2;
-    const int x = bx * kBX + threadIdx.x, y = by * kBY + threadIdx.y;
-    const int z0 = bz * V.zc, z1 = min(z0 + V.zc, d0);
-    if (x >= d2 || y >= d1) return;
-    const int s0 = d1 * d2;
-    const bool yin = y < d1 - 1, xin = x < d2 - 1;
-    const float ss0 = V.ss0, ss1 = V.ss1, ss2 = V.ss2;
-    const float sq[3] = {G.sq0, G.sq1, G.sq2};
-    const float isq[3] = {G.isq0, G.isq1, G.isq2};
-    const float4 w4 = G.w, n4 = G.nid2;
-    const int64_t S = G.slab;
-    float4 *__restrict__ hp0 = G.state;
-    float4 *__restrict__ hp1 = hp0 + S;
-    float4 *__restrict__ hp2 = hp1 + S;
-    const float4 *__restrict__ tmp = hp0 + 4 * S;
-    const float4 *__restrict__ al4 = hp0 + kFields * S;
-    const float4 *__restrict__ q4 = V.q4;
-    const float *__restrict__ grad2 = V.grad2;
-    for (int z = z0; z < z1; ++z) {
-        const int i = (z * d1 + y) * d2 + x;
-        const bool zin = z < d0 - 1;
-        const float4 q = __ldg(q4 + i);
-        float4 a4;
-        float g2 = 0.f;
-        if (ALPHA_ARR) a4 = __ldg(al4 + i);
-        else g2 = __ldg(grad2 + i);
-        const float4 tc = __ldg(tmp + i);
-        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 tz = zin ? __ldg(tmp + i + s0) : zero;
-        const float4 ty = yin ? __ldg(tmp + i + d2) : zero;
-        const float4 tx = xin ? __ldg(tmp + i + 1) : zero;
-        const float4 h0 = hp0[i], h1 = hp1[i], h2 = hp2[i];
-        const Rot R = quat2rot(q);
-        float o0[kLanes], o1[kLanes], o2[kLanes];
-#pragma unroll
-        for (int l = 0; l < kLanes; ++l) {
-            const float c = lane_of(tc, l);
-            const float3 gr = make_float3(zin ? (lane_of(tz, l) - c) * ss0 : 0.f,
-                                          yin ? (lane_of(ty, l) - c) * ss1 : 0.f,
-                                          xin ? (lane_of(tx, l) - c) * ss2 : 0.f);
-            const float rad = ALPHA_ARR ? lane_of(a4, l) : lane_of(w4, l) * expf(lane_of(n4, l) * g2);
-            const float3 rg = rot_t(R, gr);
-            const float3 rh = rot_t(R, make_float3(lane_of(h0, l), lane_of(h1, l), lane_of(h2, l)));
-            float3 p = make_float3(rh.x * isq[0] + rg.x * sq[0], rh.y * isq[1] + rg.y * sq[1],
-                                   rh.z * isq[2] + rg.z * sq[2]);
-            const float nrm = sqrtf(p.x * p.x + p.y * p.y + p.z * p.z);
-            const float sc = nrm > rad ? rad / nrm : 1.f;
-            p = make_float3(p.x * sc * sq[0], p.y * sc * sq[1], p.z * sc * sq[2]);
-            const float3 h = rot(R, p);
-            o0[l] = h.x;
-            o1[l] = h.y;
-            o2[l] = h.z;
-        }
-        hp0[i] = make_float4(o0[0], o0[1], o0[2], o0[3]);
-        hp1[i] = make_float4(o1[0], o1[1], o1[2], o1[3]);
-        hp2[i] = make_float4(o2[0], o2[1], o2[2], o2[3]);
-    }
-}
-
-// U with update_tmp fused (update_qp.cl:241-300, :311-316) for the four lanes
-// of a group; a stopped lane keeps its u.  On check iterations the block's
-// per-lane sum of |err| goes to partials[part_off + tile] (fixed order).
-template <bool CHECK>
-__global__ void __launch_bounds__(kTile, M16_BATCH_MINB) bt_label_kernel(const int2 *__restrict__ work,
-                                                                        const VolDev *vols, const GroupDev *groups,
-                                                                        const unsigned *__restrict__ gmask,
-                                                                        float4 *__restrict__ partials)
-{
-    __shared__ float4 red[kTile / 32];
-    const int2 wk = work[blockIdx.x];
-    const unsigned stopped = __ldcg(gmask + wk.x);
-    if (stopped == kAllLanes) return;   // uniform over the block
-    const GroupDev &G = groups[wk.x];
-    const VolDev &V = vols[G.vol];
-    int bx, by, bz;
-    decode_tile(V, wk.y, bx, by, bz);
-    const int d0 = V.d0, d1 = V.d1, d2 = V.d2;
-    const int x = bx * kBX + threadIdx.x, y = by * kBY + threadIdx.y;
-    const int z0 = bz * V.zc, z1 = min(z0 + V.zc, d0);
-    float acc[kLanes] = {0.f, 0.f, 0.f, 0.f};
-    if (x < d2 && y < d1) {
-        const int s0 = d1 * d2;
-        const bool ylo = y > 0, xlo = x > 0, yhi = y < d1 - 1, xhi = x < d2 - 1;
-        const float rcc = V.rcc, rs0 = V.rs0, rs1 = V.rs1, rs2 = V.rs2;
-        const int64_t S = G.slab;
-        const float4 *__restrict__ hp0 = G.state;
-        const float4 *__restrict__ hp1 = hp0 + S;
-        const float4 *__restrict__ hp2 = hp1 + S;
-        float4 *__restrict__ ptp = G.state + 3 * S;
-        float4 *__restrict__ tmp = G.state + 4 * S;
-        float4 *__restrict__ up = G.state + 5 * S;
-        const float *__restrict__ csp = V.cs;
-        const float *__restrict__ ctp = V.ct;
-        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int z = z0; z < z1; ++z) {
-            const int i = (z * d1 + y) * d2 + x;
-            const float4 h0 = __ldg(hp0 + i), h1 = __ldg(hp1 + i), h2 = __ldg(hp2 + i);
-            const float4 h0m = z > 0 ? __ldg(hp0 + i - s0) : zero;
-            const float4 h1m = ylo ? __ldg(hp1 + i - d2) : zero;
-            const float4 h2m = xlo ? __ldg(hp2 + i - 1) : zero;
-            const float4 uo = up[i], pto = ptp[i];
-            const float csv = __ldg(csp + i), ctv = __ldg(ctp + i);
-            const bool zhi = z < d0 - 1;
-            float on[kLanes], op[kLanes], ot[kLanes];
-#pragma unroll
-            for (int l = 0; l < kLanes; ++l) {
-                const float div = ((zhi ? lane_of(h0, l) : 0.f) - lane_of(h0m, l)) * rs0 +
-                                  ((yhi ? lane_of(h1, l) : 0.f) - lane_of(h1m, l)) * rs1 +
-                                  ((xhi ? lane_of(h2, l) : 0.f) - lane_of(h2m, l)) * rs2;
-                const float u0 = lane_of(uo, l);
-                const float psx = div + lane_of(pto, l) - rcc * (u0 - 1.f);
-                const float ps = csv < psx ? csv : psx;
-                const float ptx = -div + ps + rcc * u0;
-                const float ptn = ctv < ptx ? ctv : ptx;
-                const float err = div - ps + ptn;
-                const float un = u0 - err / rcc;
-                op[l] = ptn;
-                on[l] = (stopped >> l) & 1u ? u0 : un;
-                ot[l] = err - un * rcc;
-                if (CHECK) acc[l] += fabsf(err);
-            }
-            ptp[i] = make_float4(op[0], op[1], op[2], op[3]);
-            up[i] = make_float4(on[0], on[1], on[2], on[3]);
-            tmp[i] = make_float4(ot[0], ot[1], ot[2], ot[3]);
-        }
-    }
-    if (CHECK) {
-        const int tid = threadIdx.x + kBX * threadIdx.y;
-#pragma unroll
-        for (int l = 0; l < kLanes; ++l)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc[l] += __shfl_down_sync(0xffffffffu, acc[l], o);
-        if ((tid & 31) == 0) red[tid >> 5] = make_float4(acc[0], acc[1], acc[2], acc[3]);
-        __syncthreads();
-        if (tid == 0) {
-            float4 s = red[0];
-            for (int w = 1; w < kTile / 32; ++w) {
-                s.x += red[w].x; s.y += red[w].y; s.z += red[w].z; s.w += red[w].w;
-            }
-            partials[G.part_off + wk.y] = s;
-        }
-    }
-}
-
-// one block per instance: residual = sum over the tiles of its lane's partial
-// sums / (N * rcc); below the bound (or NaN) the instance stops
-__global__ void bt_check_kernel(const VolDev *vols, const GroupDev *groups, const InstDev *insts,
-                                InstCtrl *ctrl, unsigned *gmask, const float4 *__restrict__ partials, double bound,
-                                int iter)
-{
-    __shared__ double s[256];
-    const InstDev &I = insts[blockIdx.x];
-    InstCtrl &C = ctrl[blockIdx.x];
-    if (__ldcg(&C.stopped)) return;
-    const GroupDev &G = groups[I.group];
-    const VolDev &V = vols[G.vol];
-    const float *p = (const float *)(partials + G.part_off) + I.lane;
-    double acc = 0.0;
-    for (int k = threadIdx.x; k < G.nparts; k += blockDim.x) acc += (double)p[4 * k];
-    s[threadIdx.x] = acc;
-    __syncthreads();
-    for (int w = blockDim.x >> 1; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const double err = s[0] / ((double)V.n * (double)V.rcc);
-        C.resid = err;
-        C.n_checks += 1;
-        if (isnan(err) || err < bound) {
-            C.stopped = 1;
-            C.iterations = iter + 1;
-            atomicOr(gmask + I.group, 1u << I.lane);
-        }
-    }
-}
 
 // ---- host side --------------------------------------------------------------
 
 struct Plan {
     std::vector<int> inst_group, inst_lane;       // per instance
     std::vector<std::vector<int>> group_insts;    // per group: instance per lane (-1 padding)
-    std::vector<int> group_vol;
+    std::vector<int> group_vol, group_lanes;
     std::vector<int> ngroups_of_vol;
 };
 
 // groups: instances of one volume with the same eigenvalues and the same kind
-// of alpha, in instance order, four to a group
+// of alpha, in instance order, four to a group; a group that would hold fewer
+// than three instances becomes one-lane groups (padding lanes would stream
+// more than the shared volume data saves)
 inline Plan make_plan(int nvol, const m16_batch_instance *inst, int ninst)
 {
+    Plan Q;   // four-lane grouping first
+    Q.inst_group.assign(ninst, -1);
+    Q.inst_lane.assign(ninst, -1);
+    {
+        std::map<std::tuple<int, double, double, double, int>, int> open;
+        for (int i = 0; i < ninst; ++i) {
+            const m16_batch_instance &I = inst[i];
+            const auto key = std::make_tuple(I.volume, I.sqevals[0], I.sqevals[1], I.sqevals[2], I.alpha ? 1 : 0);
+            auto it = open.find(key);
+            int g;
+            if (it == open.end()) {
+                g = (int)Q.group_insts.size();
+                Q.group_insts.push_back(std::vector<int>(kLanes, -1));
+                open[key] = g;
+            } else {
+                g = it->second;
+            }
+            int lane = 0;
+            while (Q.group_insts[g][lane] >= 0) ++lane;
+            Q.group_insts[g][lane] = i;
+            if (lane == kLanes - 1) open.erase(key);
+        }
+    }
     Plan P;
     P.inst_group.assign(ninst, -1);
     P.inst_lane.assign(ninst, -1);
     P.ngroups_of_vol.assign(nvol, 0);
-    std::map<std::tuple<int, double, double, double, int>, int> open;   // key -> group with free lanes
-    for (int i = 0; i < ninst; ++i) {
-        const m16_batch_instance &I = inst[i];
-        const auto key = std::make_tuple(I.volume, I.sqevals[0], I.sqevals[1], I.sqevals[2], I.alpha ? 1 : 0);
-        auto it = open.find(key);
-        int g;
-        if (it == open.end()) {
-            g = (int)P.group_insts.size();
-            P.group_insts.push_back(std::vector<int>(kLanes, -1));
-            P.group_vol.push_back(I.volume);
-            P.ngroups_of_vol[I.volume] += 1;
-            open[key] = g;
+    for (const std::vector<int> &lanes : Q.group_insts) {
+        int real = 0;
+        for (int i : lanes) real += i >= 0;
+        const int vol = inst[lanes[0]].volume;
+        if (real >= 3) {
+            const int g = (int)P.group_insts.size();
+            P.group_insts.push_back(lanes);
+            P.group_vol.push_back(vol);
+            P.group_lanes.push_back(kLanes);
+            P.ngroups_of_vol[vol] += 1;
+            for (int l = 0; l < kLanes; ++l)
+                if (lanes[l] >= 0) { P.inst_group[lanes[l]] = g; P.inst_lane[lanes[l]] = l; }
         } else {
-            g = it->second;
+            for (int i : lanes) {
+                if (i < 0) continue;
+                const int g = (int)P.group_insts.size();
+                std::vector<int> one(kLanes, -1);
+                one[0] = i;
+                P.group_insts.push_back(one);
+                P.group_vol.push_back(vol);
+                P.group_lanes.push_back(1);
+                P.ngroups_of_vol[vol] += 1;
+                P.inst_group[i] = g;
+                P.inst_lane[i] = 0;
+            }
         }
-        int lane = 0;
-        while (P.group_insts[g][lane] >= 0) ++lane;
-        P.group_insts[g][lane] = i;
-        P.inst_group[i] = g;
-        P.inst_lane[i] = lane;
-        if (lane == kLanes - 1) open.erase(key);
     }
     return P;
 }
@@ -429,7 +90,8 @@ inline Plan make_plan(int nvol, const m16_batch_instance *inst, int ninst)
 struct BatchLayout {
     std::vector<size_t> q4, maxpart;        // per volume
     std::vector<size_t> state;              // per group
-    std::vector<int> part_off, nparts;      // per group (float4 units)
+    std::vector<int64_t> part_off;          // per group (float4 units)
+    std::vector<int> nparts;                // per group
     size_t ctrl, gmask, vols, groups, insts, work, partials, total;
     int64_t total_blocks, total_parts;
 };
@@ -457,8 +119,11 @@ inline BatchLayout batch_layout(const m16_batch_volume *vols, int nvol, const m1
         const m16_batch_volume &V = vols[P.group_vol[g]];
         const int64_t n = (int64_t)V.d0 * V.d1 * V.d2;
         const bool has_alpha = inst[P.group_insts[g][0]].alpha != nullptr;
-        L.state.push_back(take((kFields + (has_alpha ? 1 : 0)) * align_up(n * 16, 256)));
-        L.part_off.push_back((int)L.total_parts);
+        if (P.group_lanes[g] == kLanes)
+            L.state.push_back(take((kFields + (has_alpha ? 1 : 0)) * align_up(n * 16, 256)));
+        else
+            L.state.push_back(take(kFields * align_up(n * 4, 256)));
+        L.part_off.push_back(L.total_parts);
         L.nparts.push_back((int)tiles[P.group_vol[g]]);
         L.total_parts += tiles[P.group_vol[g]];
         L.total_blocks += tiles[P.group_vol[g]];
@@ -551,6 +216,9 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         d.part_off = L.part_off[g];
         d.nparts = L.nparts[g];
         d.has_alpha = I0.alpha ? 1 : 0;
+        d.lanes = P.group_lanes[g];
+        d.pad0 = d.pad1 = d.pad2 = 0;
+        d.alpha1 = d.lanes == 1 ? I0.alpha : nullptr;
         float w[kLanes], nid2[kLanes];
         for (int l = 0; l < kLanes; ++l) {
             const int i = lanes[l];
@@ -568,8 +236,9 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         d.sq0 = (float)I0.sqevals[0]; d.sq1 = (float)I0.sqevals[1]; d.sq2 = (float)I0.sqevals[2];
         d.isq0 = (float)(1.0 / I0.sqevals[0]); d.isq1 = (float)(1.0 / I0.sqevals[1]);
         d.isq2 = (float)(1.0 / I0.sqevals[2]);
-        d.state = (float4 *)(ws + L.state[g]);
-        d.slab = (int64_t)(align_up(hv[d.vol].n * 16, 256) / 16);
+        d.state = ws + L.state[g];
+        const size_t esz = d.lanes == kLanes ? 16 : 4;
+        d.slab = (int64_t)(align_up(hv[d.vol].n * esz, 256) / esz);
     }
     std::vector<InstDev> hi(ninst);
     for (int i = 0; i < ninst; ++i) {
@@ -614,7 +283,7 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         const int blocks = (int)std::min<int64_t>(kMaxBlocks, div_up(n, 256));
         bt_init_group_kernel<<<blocks, 256, 0, st>>>(vols[hg[g].vol].img, dvols, dgroups, g);
         ++launches;
-        if (hg[g].has_alpha) {
+        if (hg[g].has_alpha && hg[g].lanes == kLanes) {
             const float *a[kLanes];
             for (int l = 0; l < kLanes; ++l)
                 a[l] = P.group_insts[g][l] >= 0 ? inst[P.group_insts[g][l]].alpha : nullptr;
@@ -624,22 +293,26 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     }
     M16_CUDA_TRY(cudaGetLastError());
 
-    // the work list: per group and tile, groups with an active lane only;
-    // alpha-field groups first (the flow sweep is compiled per alpha kind)
+    // the work list: per group and tile, groups with an active lane only, in
+    // four segments (the sweeps are compiled per group kind): four-lane with
+    // alpha fields, four-lane with (w, decay), one-lane with alpha fields,
+    // one-lane with (w, decay)
     std::vector<char> gactive(ngroups, 1);
     for (int g = 0; g < ngroups; ++g) gactive[g] = hmask[g] != kAllLanes;
-    int n_alpha_items = 0;
+    int seg[5] = {0, 0, 0, 0, 0};   // segment k: items seg[k] .. seg[k + 1] - 1
+    auto kind_of = [&](int g) { return (hg[g].lanes == kLanes ? 0 : 2) + (hg[g].has_alpha ? 0 : 1); };
     auto build_work = [&](std::vector<int2> &w) {
         w.clear();
-        for (int pass = 0; pass < 2; ++pass) {
+        for (int k = 0; k < 4; ++k) {
+            seg[k] = (int)w.size();
             for (int g = 0; g < ngroups; ++g) {
-                if (!gactive[g] || (hg[g].has_alpha != 0) != (pass == 0)) continue;
+                if (!gactive[g] || kind_of(g) != k) continue;
                 const VolDev &V = hv[hg[g].vol];
                 const int ntiles = V.tx * V.ty * V.tz;
                 for (int t = 0; t < ntiles; ++t) w.push_back(make_int2(g, t));
             }
-            if (pass == 0) n_alpha_items = (int)w.size();
         }
+        seg[4] = (int)w.size();
     };
     std::vector<int2> work;
     build_work(work);
@@ -662,18 +335,28 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     const dim3 block(kBX, kBY, 1);
     while (it < params->num_iter && n_groups_active > 0 && !work.empty()) {
         const int end = std::min(params->num_iter, it + chunk);
-        const int nb_alpha = n_alpha_items;
-        const int nb_exp = (int)work.size() - n_alpha_items;
         for (; it < end; ++it) {
             if (timing) cudaEventRecord(e0, st);
             const bool check = (it % update) == 0;
-            if (nb_alpha > 0) bt_flow_kernel<true><<<nb_alpha, block, 0, st>>>(dwork, dvols, dgroups, dmask);
-            if (nb_exp > 0) bt_flow_kernel<false><<<nb_exp, block, 0, st>>>(dwork + nb_alpha, dvols, dgroups, dmask);
+            const int n4 = seg[2], n1 = seg[4] - seg[2];
+            if (seg[1] > seg[0])
+                bt_flow_kernel<true><<<seg[1] - seg[0], block, 0, st>>>(dwork + seg[0], dvols, dgroups, dmask);
+            if (seg[2] > seg[1])
+                bt_flow_kernel<false><<<seg[2] - seg[1], block, 0, st>>>(dwork + seg[1], dvols, dgroups, dmask);
+            if (seg[3] > seg[2])
+                bt1_flow_kernel<kAlphaArray><<<seg[3] - seg[2], block, 0, st>>>(dwork + seg[2], dvols, dgroups, dmask);
+            if (seg[4] > seg[3])
+                bt1_flow_kernel<kAlphaFromGrad2><<<seg[4] - seg[3], block, 0, st>>>(dwork + seg[3], dvols, dgroups,
+                                                                                 dmask);
             if (timing) cudaEventRecord(e1, st);
-            if (check)
-                bt_label_kernel<true><<<(unsigned)work.size(), block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
-            else
-                bt_label_kernel<false><<<(unsigned)work.size(), block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
+            if (n4 > 0) {
+                if (check) bt_label_kernel<true><<<n4, block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
+                else bt_label_kernel<false><<<n4, block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
+            }
+            if (n1 > 0) {
+                if (check) bt1_label_kernel<true><<<n1, block, 0, st>>>(dwork + seg[2], dvols, dgroups, dmask, dpart);
+                else bt1_label_kernel<false><<<n1, block, 0, st>>>(dwork + seg[2], dvols, dgroups, dmask, dpart);
+            }
             if (timing) {
                 cudaEventRecord(e2, st);
                 M16_CUDA_TRY(cudaEventSynchronize(e2));
@@ -683,10 +366,11 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
                 p_ms += a; ++p_n;
                 u_ms += b; ++u_n;
             }
-            launches += (nb_alpha > 0) + (nb_exp > 0) + 1;
+            for (int k = 0; k < 4; ++k) launches += seg[k + 1] > seg[k];
+            launches += (n4 > 0) + (n1 > 0);
             if (check) {
                 bt_check_kernel<<<ninst, 256, 0, st>>>(dvols, dgroups, dinsts, dctrl, dmask, dpart,
-                                                       params->error_bound, it);
+                                                       params->error_bound, update, nullptr);
                 ++launches;
             }
         }

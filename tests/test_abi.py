@@ -89,3 +89,27 @@ def test_solve_ex_rejects_an_unknown_iteration_path(lib):
         st = lib.m16_maxflow_solve_ex(fake, fake, sq, None, None, 0.1, fake, fake, None, 4, 4, 4, ctypes.byref(p),
                                       fake, ctypes.byref(it), None, 0, None, fake, 1 << 20, None, ctypes.byref(s))
         assert st == N.M16_ERR_BAD_ARG
+
+
+def test_server_create_validates_before_touching_the_gpu(lib):
+    from miccai2016_gb300 import _native as N
+    h = ctypes.c_void_p()
+    p = N.CutParams(0.2, 0.11, 1e-4, 100, 30, (ctypes.c_double * 3)(1, 1, 1))   # 100 is not a multiple of 30
+    assert lib.m16_server_create(ctypes.byref(p), 4, 1024, ctypes.c_void_p(256), 1 << 30, None,
+                                 ctypes.byref(h)) == N.M16_ERR_BAD_ARG
+    p.num_iter = 90
+    assert lib.m16_server_create(ctypes.byref(p), 4, 1024, None, 1 << 30, None, ctypes.byref(h)) == N.M16_ERR_WORKSPACE
+    assert lib.m16_server_create(ctypes.byref(p), 4, 1024, ctypes.c_void_p(256), 16, None,
+                                 ctypes.byref(h)) == N.M16_ERR_WORKSPACE
+    assert lib.m16_server_create(ctypes.byref(p), 0, 1024, ctypes.c_void_p(256), 1 << 30, None,
+                                 ctypes.byref(h)) == N.M16_ERR_BAD_ARG
+    assert not h.value
+
+
+def test_server_sizes(lib):
+    # a resident request holds its inputs (28 B), the expanded quaternions
+    # (16 B) and six state fields (24 B) per voxel, plus small per-tile parts
+    b = lib.m16_server_request_bytes(64, 64, 64, 0)
+    assert 68 * 64 ** 3 <= b <= 68 * 64 ** 3 + (1 << 20)
+    assert lib.m16_server_request_bytes(0, 64, 64, 0) == 0
+    assert lib.m16_server_table_bytes(16, 1024) > 0
