@@ -364,6 +364,20 @@ int m16_complete_transformations(const float *dirs3, int64_t n, float *quat3, vo
 int m16_adjust_nonridge_signs(float *dirs3, int32_t d0, int32_t d1, int32_t d2, const uint16_t *coords,
                               const float *rdirs, int64_t num_ridge, const double *scaling3, void *stream);
 
+/* Workspace bytes of m16_adjust_nonridge_signs_indexed (0 for invalid sizes). */
+size_t m16_adjust_nonridge_signs_workspace_bytes(int32_t d0, int32_t d1, int32_t d2, int64_t num_ridge);
+
+/* The same sign flips as m16_adjust_nonridge_signs -- bit for bit, the same
+ * nearest ridge point with the same lowest-index tie-break -- found through a
+ * cell index of the ridge points built in the workspace, so the cost grows
+ * with the points near each voxel instead of with N x num_ridge.  Replaces the
+ * same reference interface (adjust_directions.py:419-446,
+ * adjust_directions.cl:182-246).  d0 <= 65535, num_ridge <= 2^31 - 1;
+ * coordinates beyond the volume are allowed. */
+int m16_adjust_nonridge_signs_indexed(float *dirs3, int32_t d0, int32_t d1, int32_t d2, const uint16_t *coords,
+                                      const float *rdirs, int64_t num_ridge, const double *scaling3,
+                                      void *workspace, size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,7 +9,8 @@ GPU, the minimum spanning tree over the ridge points and the sign propagation
 along it on the host (ridge_mst.py: SciPy's Kruskal tree with a stable order
 of equal distances, without the reference's dense R x R matrix), ridge
 cleaning on the host, and the nearest-ridge sign flip of every voxel on the
-GPU (m16_adjust_nonridge_signs).  TransformationCompleter
+GPU (m16_adjust_nonridge_signs_indexed: the reference's brute-force nearest
+ridge point, found through a cell index of the ridge points).  TransformationCompleter
 runs m16_complete_transformations.
 """
 from __future__ import annotations
@@ -216,9 +217,11 @@ class AdvancedAdjuster(TreePrintable):
         rdirs = N.to_device_f32(ridge_dirs)
         d0, d1, d2 = self.response.shape
         sc = (ctypes.c_double * 3)(*[float(v) for v in self.voxel_size])
-        st = N.lib().m16_adjust_nonridge_signs(N.ptr(self._d_qeigs), d0, d1, d2, N.ptr(coords), N.ptr(rdirs),
-                                              len(ridge_coords), sc, N.stream_ptr())
-        N.check("m16_adjust_nonridge_signs", st)
+        L = N.lib()
+        ws = N.workspace(L.m16_adjust_nonridge_signs_workspace_bytes(d0, d1, d2, len(ridge_coords)))
+        st = L.m16_adjust_nonridge_signs_indexed(N.ptr(self._d_qeigs), d0, d1, d2, N.ptr(coords), N.ptr(rdirs),
+                                                 len(ridge_coords), sc, N.ptr(ws), ws.numel(), N.stream_ptr())
+        N.check("m16_adjust_nonridge_signs_indexed", st)
         return self._d_qeigs.cpu().numpy()
 
 

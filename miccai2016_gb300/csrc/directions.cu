@@ -13,6 +13,7 @@
 #include <float.h>
 
 #include <algorithm>
+#include <climits>
 
 #include "common.cuh"
 
@@ -27,10 +28,13 @@ __device__ __forceinline__ void qexpand_ref(float phi, float theta, float psi, f
 {
     const float pp = __fmul_rn(__fadd_rn(phi, psi), 0.5f);
     const float pm = __fmul_rn(__fsub_rn(phi, psi), 0.5f);
-    const float ct = (float)cos((double)theta * 0.5);
-    const float st = (float)sin((double)theta * 0.5);
-    const float cpp = (float)cos((double)pp), spp = (float)sin((double)pp);
-    const float cpm = (float)cos((double)pm), spm = (float)sin((double)pm);
+    double s, c;
+    sincos((double)theta * 0.5, &s, &c);
+    const float ct = (float)c, st = (float)s;
+    sincos((double)pp, &s, &c);
+    const float cpp = (float)c, spp = (float)s;
+    sincos((double)pm, &s, &c);
+    const float cpm = (float)c, spm = (float)s;
     q[0] = __fmul_rn(cpp, ct);
     q[1] = __fmul_rn(cpm, st);
     q[2] = __fmul_rn(spm, st);
@@ -261,6 +265,247 @@ __global__ void __launch_bounds__(256) dr_adjust_kernel(float *__restrict__ dirs
     }
 }
 
+// ---- adjustNonRidgeSigns over a cell index ----------------------------------------
+// The same nearest ridge point (smallest distance, then smallest index) found
+// without visiting every point: the ridge points are bucketed into cubic cells
+// of c voxels a side, and each voxel scans Chebyshev shells of cells around
+// its own cell.  A cell is skipped only when a lower bound of every distance
+// in it exceeds the best distance so far, and the scan ends when the bound of
+// everything outside the scanned block does; both bounds are evaluated with
+// the distance's own rounded operations on the smallest possible per-axis
+// offsets, and every rounded operation involved is monotone, so no point
+// that could win (ties included) is ever skipped.  Equal distances resolve
+// by comparing indices, so the order of the points inside a cell is free.
+struct CellGrid {
+    int c;                 // cell side in voxels
+    int g0, g1, g2;        // cells per axis
+    int d0, d1, d2;        // the volume (coordinates beyond it are clamped into its last cells)
+    int64_t ncells;
+};
+
+constexpr int64_t kMaxCells = (int64_t)1 << 22;   // the two-level scan covers 4096 x 1024 cells
+
+inline CellGrid make_cell_grid(int d0, int d1, int d2, int64_t R)
+{
+    const double n = (double)d0 * d1 * d2;
+    // about four ridge points per cell on average
+    int c = (int)ceil(cbrt(4.0 * n / (double)std::max<int64_t>(R, 1)));
+    c = std::max(2, std::min(c, 1 << 16));
+    CellGrid g;
+    g.d0 = d0; g.d1 = d1; g.d2 = d2;
+    for (;; ++c) {
+        g.c = c;
+        g.g0 = (int)div_up(d0, c); g.g1 = (int)div_up(d1, c); g.g2 = (int)div_up(d2, c);
+        g.ncells = (int64_t)g.g0 * g.g1 * g.g2;
+        if (g.ncells <= kMaxCells) break;
+    }
+    return g;
+}
+
+constexpr int kScanItems = 1024;   // cells per scan block (256 threads x 4)
+
+struct NrLayout {
+    size_t count, start, bsum, pts, total;
+    int64_t nblocks;
+};
+
+inline NrLayout nr_layout(const CellGrid &g, int64_t R)
+{
+    NrLayout L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
+    L.nblocks = div_up(g.ncells, kScanItems);
+    L.count = take((size_t)g.ncells * 4);
+    L.start = take((size_t)(g.ncells + 1) * 4);
+    L.bsum = take((size_t)(L.nblocks + 1) * 4);
+    L.pts = take((size_t)R * 16);
+    L.total = off;
+    return L;
+}
+
+// cell of a ridge point; a coordinate beyond the volume goes to the last cell
+// of its axis (its distances only grow, so every bound stays a bound)
+__device__ __forceinline__ int64_t cell_of(int a0, int a1, int a2, CellGrid g)
+{
+    a0 = min(a0, g.d0 - 1); a1 = min(a1, g.d1 - 1); a2 = min(a2, g.d2 - 1);
+    return ((int64_t)(a0 / g.c) * g.g1 + a1 / g.c) * g.g2 + a2 / g.c;
+}
+
+__global__ void nr_count_kernel(const uint16_t *__restrict__ coords, int64_t R, CellGrid g,
+                                unsigned *__restrict__ count)
+{
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < R; j += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(count + cell_of(coords[3 * j], coords[3 * j + 1], coords[3 * j + 2], g), 1u);
+}
+
+// exclusive scan of the counts, in blocks of kScanItems: local scan + block sums
+__global__ void __launch_bounds__(256) nr_scan_local_kernel(const unsigned *__restrict__ count, int64_t ncells,
+                                                            unsigned *__restrict__ start, unsigned *__restrict__ bsum)
+{
+    __shared__ unsigned s[256];
+    const int64_t base = blockIdx.x * (int64_t)kScanItems + 4 * threadIdx.x;
+    unsigned v[4], t = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        v[k] = base + k < ncells ? count[base + k] : 0u;
+        t += v[k];
+    }
+    s[threadIdx.x] = t;
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {   // inclusive Hillis-Steele over the thread totals
+        const unsigned add = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0u;
+        __syncthreads();
+        s[threadIdx.x] += add;
+        __syncthreads();
+    }
+    unsigned run = s[threadIdx.x] - t;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < ncells) start[base + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 255) bsum[blockIdx.x] = s[255];
+}
+
+// exclusive scan of the block sums in place (one block; nblocks <= 4096)
+__global__ void __launch_bounds__(1024) nr_scan_blocks_kernel(unsigned *bsum, int64_t nblocks)
+{
+    __shared__ unsigned s[1024];
+    unsigned v[4], t = 0;
+    const int64_t base = 4 * (int64_t)threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        v[k] = base + k < nblocks ? bsum[base + k] : 0u;
+        t += v[k];
+    }
+    s[threadIdx.x] = t;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const unsigned add = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0u;
+        __syncthreads();
+        s[threadIdx.x] += add;
+        __syncthreads();
+    }
+    unsigned run = s[threadIdx.x] - t;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < nblocks) bsum[base + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 1023) bsum[nblocks] = s[1023];
+}
+
+// start[i] += offset of its block; start[ncells] = R; counts reset to 0 (the
+// scatter reuses them as fill counters)
+__global__ void nr_scan_add_kernel(unsigned *__restrict__ start, unsigned *__restrict__ count,
+                                   const unsigned *__restrict__ bsum, int64_t ncells, int64_t nblocks)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= ncells; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i == ncells) { start[i] = bsum[nblocks]; continue; }
+        start[i] += bsum[i / kScanItems];
+        count[i] = 0u;
+    }
+}
+
+__global__ void nr_scatter_kernel(const uint16_t *__restrict__ coords, int64_t R, CellGrid g,
+                                  const unsigned *__restrict__ start, unsigned *__restrict__ fill,
+                                  float4 *__restrict__ pts)
+{
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < R; j += (int64_t)gridDim.x * blockDim.x) {
+        const int a0 = coords[3 * j], a1 = coords[3 * j + 1], a2 = coords[3 * j + 2];
+        const int64_t c = cell_of(a0, a1, a2, g);
+        const unsigned pos = start[c] + atomicAdd(fill + c, 1u);
+        pts[pos] = make_float4((float)a0, (float)a1, (float)a2, __int_as_float((int)j));
+    }
+}
+
+// the reference's distance: ((|dp0| s0)^2 + (|dp1| s1)^2) + (|dp2| s2)^2, each step rounded
+__device__ __forceinline__ float ref_dist(float f0, float f1, float f2)
+{
+    return __fadd_rn(__fadd_rn(__fmul_rn(f0, f0), __fmul_rn(f1, f1)), __fmul_rn(f2, f2));
+}
+
+// lower bound of the rounded squared term of an axis for every point outside
+// cells [clo, chi] of that axis (infinite when the block reaches both ends)
+__device__ __forceinline__ float block_gap(int p, int clo, int chi, int ncell, int c, float s)
+{
+    float o = INFINITY;
+    if (clo > 0) o = fminf(o, __fmul_rn((float)(p - clo * c + 1), s));
+    if (chi < ncell - 1) o = fminf(o, __fmul_rn((float)((chi + 1) * c - p), s));
+    return o == INFINITY ? INFINITY : __fmul_rn(o, o);
+}
+
+// smallest |p - c| over integer c in [lo, hi] (0 inside), times s, rounded
+__device__ __forceinline__ float axis_gap(int p, int lo, int hi, float s)
+{
+    const int m = p < lo ? lo - p : (p > hi ? p - hi : 0);
+    return __fmul_rn((float)m, s);
+}
+
+__global__ void __launch_bounds__(kBX * kBY) dr_adjust_indexed_kernel(
+    float *__restrict__ dirs3, const float4 *__restrict__ pts, const unsigned *__restrict__ start,
+    const float *__restrict__ rdirs, CellGrid g, int d0, int d1, int d2, float s0, float s1, float s2)
+{
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y * kBY + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= d2 || y >= d1) return;
+    const float p0 = (float)z, p1 = (float)y, p2 = (float)x;
+    const int cz = z / g.c, cy = y / g.c, cx = x / g.c;
+    float best = INFINITY;
+    int bj = INT_MAX;
+    const int rmax = max(max(max(cz, g.g0 - 1 - cz), max(cy, g.g1 - 1 - cy)), max(cx, g.g2 - 1 - cx));
+    for (int r = 0; r <= rmax; ++r) {
+        for (int dz = -r; dz <= r; ++dz) {
+            const int qz = cz + dz;
+            if (qz < 0 || qz >= g.g0) continue;
+            const float gz = axis_gap(z, qz * g.c, qz * g.c + g.c - 1, s0);
+            for (int dy = -r; dy <= r; ++dy) {
+                const int qy = cy + dy;
+                if (qy < 0 || qy >= g.g1) continue;
+                const float gy = axis_gap(y, qy * g.c, qy * g.c + g.c - 1, s1);
+                const bool face = dz == -r || dz == r || dy == -r || dy == r;
+                const int step = face ? 1 : 2 * r;   // off the faces only dx = -r and dx = r lie on the shell
+                for (int dx = -r; dx <= r; dx += step) {
+                    const int qx = cx + dx;
+                    if (qx >= 0 && qx < g.g2) {
+                        const float gx = axis_gap(x, qx * g.c, qx * g.c + g.c - 1, s2);
+                        if (!(ref_dist(gz, gy, gx) > best)) {
+                            const int64_t cell = ((int64_t)qz * g.g1 + qy) * g.g2 + qx;
+                            const unsigned e = __ldg(start + cell + 1);
+                            for (unsigned k = __ldg(start + cell); k < e; ++k) {
+                                const float4 q = __ldg(pts + k);
+                                const float f0 = __fmul_rn(fabsf(__fsub_rn(p0, q.x)), s0);
+                                const float f1 = __fmul_rn(fabsf(__fsub_rn(p1, q.y)), s1);
+                                const float f2 = __fmul_rn(fabsf(__fsub_rn(p2, q.z)), s2);
+                                const float d = ref_dist(f0, f1, f2);
+                                const int j = __float_as_int(q.w);
+                                if (d < best || (d == best && j < bj)) { best = d; bj = j; }
+                            }
+                        }
+                    }
+                    if (r == 0) break;
+                }
+            }
+        }
+        // everything outside the scanned block differs on some axis by more
+        // than the block reaches on that axis (no points lie beyond the grid)
+        const float oz = fminf(block_gap(z, cz - r, cz + r, g.g0, g.c, s0), block_gap(y, cy - r, cy + r, g.g1, g.c, s1));
+        const float lo = fminf(oz, block_gap(x, cx - r, cx + r, g.g2, g.c, s2));
+        if (lo > best) break;
+    }
+    if (bj == INT_MAX) return;
+    float *v = dirs3 + 3 * (((int64_t)z * d1 + y) * d2 + x);
+    const float w0 = __ldg(rdirs + 3 * (int64_t)bj), w1 = __ldg(rdirs + 3 * (int64_t)bj + 1),
+                w2 = __ldg(rdirs + 3 * (int64_t)bj + 2);
+    const float dot = __fadd_rn(__fadd_rn(__fmul_rn(v[0], w0), __fmul_rn(v[1], w1)), __fmul_rn(v[2], w2));
+    if (dot < 0.f) {
+        v[0] = -v[0];
+        v[1] = -v[1];
+        v[2] = -v[2];
+    }
+}
+
 inline int blocks1d(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(16 * kSMs, div_up(n, 256))); }
 
 }  // namespace
@@ -309,6 +554,43 @@ extern "C" int m16_adjust_nonridge_signs(float *dirs3, int32_t d0, int32_t d1, i
     dr_adjust_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(dirs3, coords, rdirs, num_ridge, d0, d1, d2,
                                                                (float)scaling3[0], (float)scaling3[1],
                                                                (float)scaling3[2]);
+    M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}
+
+extern "C" size_t m16_adjust_nonridge_signs_workspace_bytes(int32_t d0, int32_t d1, int32_t d2, int64_t num_ridge)
+{
+    if (d0 < 1 || d1 < 1 || d2 < 1 || num_ridge < 1) return 0;
+    return nr_layout(make_cell_grid(d0, d1, d2, num_ridge), num_ridge).total;
+}
+
+extern "C" int m16_adjust_nonridge_signs_indexed(float *dirs3, int32_t d0, int32_t d1, int32_t d2,
+                                                 const uint16_t *coords, const float *rdirs, int64_t num_ridge,
+                                                 const double *scaling3, void *workspace, size_t workspace_bytes,
+                                                 void *stream)
+{
+    if (d0 < 1 || d1 < 1 || d2 < 1 || d0 > 65535) return M16_ERR_BAD_SHAPE;
+    if (!dirs3 || !scaling3 || num_ridge < 1 || num_ridge > (int64_t)INT32_MAX || !coords || !rdirs)
+        return M16_ERR_BAD_ARG;
+    for (int k = 0; k < 3; ++k)
+        if (!(scaling3[k] > 0.0) || !isfinite(scaling3[k])) return M16_ERR_BAD_ARG;
+    const CellGrid g = make_cell_grid(d0, d1, d2, num_ridge);
+    const NrLayout L = nr_layout(g, num_ridge);
+    if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *ws = (char *)workspace;
+    unsigned *count = (unsigned *)(ws + L.count), *start = (unsigned *)(ws + L.start), *bsum = (unsigned *)(ws + L.bsum);
+    float4 *pts = (float4 *)(ws + L.pts);
+    M16_CUDA_TRY(cudaMemsetAsync(count, 0, (size_t)g.ncells * 4, st));
+    nr_count_kernel<<<blocks1d(num_ridge), 256, 0, st>>>(coords, num_ridge, g, count);
+    nr_scan_local_kernel<<<(unsigned)L.nblocks, 256, 0, st>>>(count, g.ncells, start, bsum);
+    nr_scan_blocks_kernel<<<1, 1024, 0, st>>>(bsum, L.nblocks);
+    nr_scan_add_kernel<<<blocks1d(g.ncells + 1), 256, 0, st>>>(start, count, bsum, g.ncells, L.nblocks);
+    nr_scatter_kernel<<<blocks1d(num_ridge), 256, 0, st>>>(coords, num_ridge, g, start, count, pts);
+    const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)d0);
+    dr_adjust_indexed_kernel<<<grid, dim3(kBX, kBY, 1), 0, st>>>(dirs3, pts, start, rdirs, g, d0, d1, d2,
+                                                                (float)scaling3[0], (float)scaling3[1],
+                                                                (float)scaling3[2]);
     M16_CUDA_TRY(cudaGetLastError());
     return M16_OK;
 }

@@ -113,3 +113,24 @@ def test_server_sizes(lib):
     assert 68 * 64 ** 3 <= b <= 68 * 64 ** 3 + (1 << 20)
     assert lib.m16_server_request_bytes(0, 64, 64, 0) == 0
     assert lib.m16_server_table_bytes(16, 1024) > 0
+
+
+def test_indexed_sign_flip_validates_before_touching_the_gpu(lib):
+    from miccai2016_gb300 import _native as N
+    fake = ctypes.c_void_p(256)
+    sc = (ctypes.c_double * 3)(1, 1, 1)
+    nb = lib.m16_adjust_nonridge_signs_workspace_bytes(64, 64, 64, 1000)
+    assert nb >= 1000 * 16
+    assert lib.m16_adjust_nonridge_signs_workspace_bytes(0, 64, 64, 1000) == 0
+    assert lib.m16_adjust_nonridge_signs_workspace_bytes(64, 64, 64, 0) == 0
+    # far fewer points than voxels -> larger cells, a smaller index
+    assert lib.m16_adjust_nonridge_signs_workspace_bytes(64, 64, 64, 10) < nb
+    call = lambda d0, R, s, ws, wsb: lib.m16_adjust_nonridge_signs_indexed(fake, d0, 64, 64, fake, fake, R, s, ws,
+                                                                           wsb, None)
+    assert call(0, 1000, sc, fake, nb) == N.M16_ERR_BAD_SHAPE
+    assert call(70000, 1000, sc, fake, nb) == N.M16_ERR_BAD_SHAPE
+    assert call(64, 0, sc, fake, nb) == N.M16_ERR_BAD_ARG
+    assert call(64, 1000, (ctypes.c_double * 3)(1, 0, 1), fake, nb) == N.M16_ERR_BAD_ARG
+    assert call(64, 1000, sc, None, nb) == N.M16_ERR_WORKSPACE
+    assert call(64, 1000, sc, fake, nb - 1) == N.M16_ERR_WORKSPACE
+    assert call(64, 1000, sc, ctypes.c_void_p(260), nb) == N.M16_ERR_WORKSPACE
