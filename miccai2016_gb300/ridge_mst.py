@@ -133,12 +133,46 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True):
     return np.concatenate([ta, ca[sel]]), np.concatenate([tb, cb[sel]])
 
 
+def _dot_signs(cur, par):
+    """Sign (-1, 0, +1; 2 for NaN) of np.dot(cur[k], par[k]) for every row k,
+    exactly as the per-row float32 np.dot of the reference's loop rounds it.
+    The float64 sum of the three (exact) float64 products has the sign of the
+    exact dot product; np.dot's float32 result can only differ from it when
+    the exact value lies within its rounding error of zero, and only those
+    rows are evaluated with np.dot itself."""
+    c64 = cur.astype(np.float64)
+    p64 = par.astype(np.float64)
+    prod = c64 * p64
+    exact = prod[:, 0] + prod[:, 1] + prod[:, 2]
+    nan = np.isnan(exact)
+    sign = np.sign(np.where(nan, 0.0, exact)).astype(np.int8)
+    sign[nan] = 2   # NaN: "np.dot(...) >= 0" fails, the point is negated whatever its parent's sign
+    # float32 sum of three products: error below 3 * 2^-23 * sum |products|
+    # (generous: covers contraction into fused multiply-adds too)
+    bound = 8.0 * 2.0 ** -23 * np.sum(np.abs(prod), axis=1)
+    unsure = np.nonzero(np.abs(exact) <= bound)[0]
+    for k in unsure:
+        d = np.dot(cur[k], par[k])
+        sign[k] = 1 if d > 0 else (-1 if d < 0 else 0)
+    return sign
+
+
 def propagate_signs(n, edges_a, edges_b, dirs, root=0):
     """Sign propagation along the tree from `root` (adjust_directions.py:382-415):
     a child keeps its direction if its dot product with its parent's adjusted
     direction is >= 0, else it is negated.  When the edges form a forest,
     every other tree is propagated from its lowest-index point, as if that
-    point were the root."""
+    point were the root.
+
+    The reference visits the points one by one.  Here all decisions are
+    evaluated at once: with s the sign a point's direction ends up with,
+    np.dot(d_c, s_p d_p) = s_p np.dot(d_c, d_p) bit for bit (negating one
+    operand negates every rounded step), so s_c = +1 where np.dot(d_c, d_p)
+    is zero (either sign of zero passes ">= 0"), s_c = -1 where it is NaN,
+    and s_c = s_p sign(np.dot(d_c, d_p)) elsewhere; the products along each
+    path to the root (or to such a restart point) are formed by pointer
+    jumping."""
+    dirs = np.asarray(dirs, dtype=np.float32)
     adjusted = np.ones((n, 3), dtype=np.float32) * np.float32(np.nan)
     g = scipy.sparse.coo_matrix((np.ones(len(edges_a)), (edges_a, edges_b)), shape=(n, n)).tocsr()
     ncomp, comp = connected_components(g, directed=False)
@@ -150,15 +184,30 @@ def propagate_signs(n, edges_a, edges_b, dirs, root=0):
         va = np.concatenate([edges_a, np.full(len(starts), root, np.int64)])
         vb = np.concatenate([edges_b, starts])
         g = scipy.sparse.coo_matrix((np.ones(len(va)), (va, vb)), shape=(n, n)).tocsr()
-    restart = np.zeros(n, bool)
-    restart[starts] = True
-    adjusted[root] = dirs[root]
     order, pred = breadth_first_order(g, root, directed=False, return_predecessors=True)
-    for c in order[1:]:
-        cur = dirs[c]
-        if restart[c]:
-            adjusted[c] = cur
-            continue
-        ref = adjusted[pred[c]]
-        adjusted[c] = cur if np.dot(cur, ref) >= 0 else -cur
+    parent = np.arange(n, dtype=np.int64)
+    val = np.ones(n, dtype=np.int8)
+    kids = order[1:]
+    kids = kids[~np.isin(kids, starts)]       # restarts keep their own direction
+    par = pred[kids].astype(np.int64)
+    e = _dot_signs(dirs[kids], dirs[par])
+    chained = (e == 1) | (e == -1)            # a zero dot restarts at +1, a NaN one at -1
+    parent[kids[chained]] = par[chained]
+    val[kids[chained]] = e[chained]
+    own = np.ones(n, dtype=np.int8)           # the absolute sign of a restart point
+    own[kids[e == 2]] = -1
+    # pointer jumping: val[c] becomes the product of the signs from c up to
+    # the first restart r (the root, a start, a zero-dot or NaN point; val of
+    # a restart stays 1, its own sign is applied once at the end)
+    while True:
+        pp = parent[parent]
+        if np.array_equal(pp, parent):
+            break
+        val = val * val[parent]
+        parent = pp
+    val = val * own[parent]
+    reached = np.zeros(n, bool)
+    reached[order] = True
+    neg = val[reached, None] < 0
+    adjusted[reached] = np.where(neg, -dirs[reached], dirs[reached])   # negation flips the sign bit, NaN too
     return adjusted
