@@ -378,6 +378,40 @@ int m16_adjust_nonridge_signs_indexed(float *dirs3, int32_t d0, int32_t d1, int3
                                       const float *rdirs, int64_t num_ridge, const double *scaling3,
                                       void *workspace, size_t workspace_bytes, void *stream);
 
+/* ---- per-volume cut inputs and scoring --------------------------------------- */
+
+/*
+ * Source / sink capacities and |grad img|^2 of a volume, replacing the
+ * experiment's host steps PhantomExperiment._calculate_bgfg_weights_for
+ * (src/phantom_experiment.py:280-301) and
+ * np.linalg.norm(np.gradient(img), axis=0) ** 2 (:345).  Evaluated in float64
+ * in the host code's operation order and rounded to float32:
+ *   r  = log((normpdf(img, 1, s^2) + eps) / (normpdf(img, 0, s^2) + eps))
+ *   cs = rq * max(r, 0)   (the foreground weights, the cut's source capacities)
+ *   ct = rq * max(-r, 0)  (the background weights, the sink capacities)
+ * with s = noise_level and rq = 1 / log((1 / sqrt(2 pi s^2) + eps) / eps);
+ * grad2 uses central differences inside and one-sided ones at the ends of
+ * each axis (every axis needs >= 2 voxels).  Any of cs, ct, grad2 may be NULL.
+ * d0 <= 65535.
+ */
+int m16_capacities(const float *img, int32_t d0, int32_t d1, int32_t d2, double noise_level, double eps, float *cs,
+                   float *ct, float *grad2, void *stream);
+
+/* Workspace bytes of m16_fast_dice for ninst segmentations. */
+size_t m16_fast_dice_workspace_bytes(int32_t ninst);
+
+/*
+ * Fast Dice of ninst segmentations against one ground truth, replacing
+ * fast_dice_for (src/phantom_experiment.py:38-49):
+ * 2 sum((u >= 0.5) * truth) / (sum(u >= 0.5) + sum(truth)), sums in float64.
+ *   u       host array of ninst device pointers, each to n floats
+ *   truth   n floats (0 / 1, or any weights as in the reference)
+ *   dice    host, ninst doubles (output)
+ * Synchronizes `stream`.
+ */
+int m16_fast_dice(const float *const *u, int32_t ninst, int64_t n, const float *truth, double *dice, void *workspace,
+                  size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

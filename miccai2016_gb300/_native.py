@@ -114,6 +114,12 @@ def _declare(L):
     L.m16_complete_transformations.argtypes = [_vp, _i64, _vp, _vp]
     L.m16_adjust_nonridge_signs.restype = ctypes.c_int
     L.m16_adjust_nonridge_signs.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp, _i64, _vp, _vp]
+    L.m16_capacities.restype = ctypes.c_int
+    L.m16_capacities.argtypes = [_vp, _i32, _i32, _i32, _f64, _f64, _vp, _vp, _vp, _vp]
+    L.m16_fast_dice_workspace_bytes.restype = _sz
+    L.m16_fast_dice_workspace_bytes.argtypes = [_i32]
+    L.m16_fast_dice.restype = ctypes.c_int
+    L.m16_fast_dice.argtypes = [ctypes.POINTER(_vp), _i32, _i64, _vp, ctypes.POINTER(_f64), _vp, _sz, _vp]
     L.m16_adjust_nonridge_signs_workspace_bytes.restype = _sz
     L.m16_adjust_nonridge_signs_workspace_bytes.argtypes = [_i32, _i32, _i32, _i64]
     L.m16_adjust_nonridge_signs_indexed.restype = ctypes.c_int

@@ -7,7 +7,7 @@ The reference experiment's per-volume preparation of the cut inputs
   sign-adjusted directions  AdvancedAdjuster.execute        (adjust_directions)
   smoothed directions       GvfGpu.execute on dirs * vesselness (gradient_vector_flow)
   quaternions of the cut    TransformationCompleter.complete
-  capacities, |grad I|^2    Gaussian log-likelihood ratio, np.gradient (host)
+  capacities, |grad I|^2    Gaussian log-likelihood ratio, np.gradient (capacities.cut_inputs)
 
 The result feeds CmfCutQAnisotropicGpu or the batched engine.
 """
@@ -19,8 +19,8 @@ import time
 
 import numpy as np
 
-from . import phantom as P
 from .adjust_directions import AdvancedAdjuster, TransformationCompleter
+from .capacities import cut_inputs
 from .gradient_vector_flow import GvfGpu, GvfParameters
 from .misc import normalize
 from .qfrangi_gpu import FeatureFilter, VesselnessCalculation
@@ -56,9 +56,8 @@ def prepare_cut_inputs(img, noise_level, scales=(1, 3, 3), ridge_thresholds=(0.0
     quats = TransformationCompleter(vdirs_smoothed).complete()
     t["complete"] = time.perf_counter() - t0
     t0 = time.perf_counter()
-    bgw, fgw = P.bgfg_weights(img, noise_level)
-    grad2 = P.grad_mag_sq(img)
+    fgw, bgw, grad2 = cut_inputs(img, noise_level)
     t["capacities"] = time.perf_counter() - t0
     f = lambda a: np.ascontiguousarray(a, dtype=np.float32)
-    return dict(quats=f(quats), fgw=f(fgw), bgw=f(bgw), grad2=f(grad2), grad2_f64=grad2,
-                vesselness=f(vesselness), ridge_points=int(adj.ridge.sum())), t
+    return dict(quats=f(quats), fgw=fgw, bgw=bgw, grad2=grad2, vesselness=f(vesselness),
+                ridge_points=int(adj.ridge.sum())), t

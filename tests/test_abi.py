@@ -134,3 +134,22 @@ def test_indexed_sign_flip_validates_before_touching_the_gpu(lib):
     assert call(64, 1000, sc, None, nb) == N.M16_ERR_WORKSPACE
     assert call(64, 1000, sc, fake, nb - 1) == N.M16_ERR_WORKSPACE
     assert call(64, 1000, sc, ctypes.c_void_p(260), nb) == N.M16_ERR_WORKSPACE
+
+
+def test_capacities_and_dice_validate_before_touching_the_gpu(lib):
+    from miccai2016_gb300 import _native as N
+    fake = ctypes.c_void_p(256)
+    cap = lambda d0, s, eps, cs, g2: lib.m16_capacities(fake, d0, 8, 8, s, eps, cs, None, g2, None)
+    assert cap(0, 1.0, 1e-9, fake, None) == N.M16_ERR_BAD_SHAPE
+    assert cap(1, 1.0, 1e-9, None, fake) == N.M16_ERR_BAD_SHAPE     # gradient needs 2 voxels per axis
+    assert cap(8, 0.0, 1e-9, fake, None) == N.M16_ERR_BAD_ARG
+    assert cap(8, 1.0, 0.0, fake, None) == N.M16_ERR_BAD_ARG
+    assert lib.m16_capacities(fake, 8, 8, 8, 1.0, 1e-9, None, None, None, None) == N.M16_ERR_BAD_ARG
+    nb = lib.m16_fast_dice_workspace_bytes(3)
+    assert nb > 0 and lib.m16_fast_dice_workspace_bytes(0) == 0
+    ptrs = (ctypes.c_void_p * 3)(256, 512, None)
+    out = (ctypes.c_double * 3)()
+    assert lib.m16_fast_dice(ptrs, 3, 100, fake, out, fake, nb, None) == N.M16_ERR_BAD_ARG   # a NULL segmentation
+    ptrs = (ctypes.c_void_p * 3)(256, 512, 768)
+    assert lib.m16_fast_dice(ptrs, 3, 100, fake, out, fake, nb - 1, None) == N.M16_ERR_WORKSPACE
+    assert lib.m16_fast_dice(ptrs, 0, 100, fake, out, fake, nb, None) == N.M16_ERR_BAD_ARG
