@@ -110,8 +110,12 @@ typedef struct m16_solve_stats {
                               iteration launches (time_kernels only) */
     double u_ms;           /* out: summed device time of the U launches (time_kernels only) */
     int32_t path;          /* in: M16_PATH_* -- how an iteration is launched */
-    int32_t reserved;
+    int32_t flags;         /* in: M16_BATCH_* options of m16_batch_solve (0 elsewhere) */
 } m16_solve_stats;
+
+/* m16_solve_stats.flags: launch every iteration directly instead of replaying
+ * CUDA graphs of whole check intervals (timed solves always launch directly). */
+#define M16_BATCH_NO_GRAPH 1
 
 /* m16_maxflow_solve with counters; stats (host) may be NULL. */
 int m16_maxflow_solve_ex(const float *img, const float *quat3, const double *sqevals3,

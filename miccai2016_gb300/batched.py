@@ -41,13 +41,14 @@ class BatchedCut(object):
                     grad2=None if grad2 is None else N.to_device_f32(grad2, shape),
                     scaling=(1.0, 1.0, 1.0) if scaling is None else tuple(float(v) for v in scaling))
 
-    def solve(self, volumes, instances, time_kernels=False, path=None):
+    def solve(self, volumes, instances, time_kernels=False, path=None, graphs=True):
         """volumes: list of prepare_volume() dicts; instances: list of dicts
         with 'volume' (index), 'eigs' (3 constant eigenvalues) and either
         ('weighting', 'decay') or 'alpha' (an array of the volume's shape).
         path is accepted for symmetry with the single solve; the batched
         engine has one iteration path (flow and label sweeps over groups of
-        four interleaved instances).
+        four interleaved instances).  graphs=False launches every iteration
+        directly instead of replaying CUDA graphs of whole check intervals.
         Returns the list of u (CUDA tensors) in instance order."""
         torch = N.torch_mod()
         L = N.lib()
@@ -83,7 +84,7 @@ class BatchedCut(object):
         iters = (ctypes.c_int32 * ni)()
         res = (ctypes.c_double * ni)()
         stats = N.SolveStats(int(bool(time_kernels)), 0, 0, 0, 0.0, 0.0,
-                             N.PATH_DEFAULT if path is None else int(path), 0)
+                             N.PATH_DEFAULT if path is None else int(path), 0 if graphs else N.BATCH_NO_GRAPH)
         st = L.m16_batch_solve(vd, nv, idesc, ni, ctypes.byref(cp), iters, res, N.ptr(self._ws), self._ws.numel(),
                                N.stream_ptr(), ctypes.byref(stats))
         N.check("m16_batch_solve", st)
@@ -109,6 +110,7 @@ def _main(argv=None):
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--iters", type=int, default=60)
     ap.add_argument("--time-kernels", action="store_true")
+    ap.add_argument("--no-graphs", action="store_true")
     a = ap.parse_args(argv)
     shape = (a.side,) * 3
     s = a.side / 128.0
@@ -126,12 +128,12 @@ def _main(argv=None):
     bc.solve([vol], insts[:1])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    bc.solve([vol], insts, time_kernels=a.time_kernels)
+    bc.solve([vol], insts, time_kernels=a.time_kernels, graphs=not a.no_graphs)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     st = bc.last_stats
     n = int(np.prod(shape))
-    out = dict(side=a.side, instances=a.instances, iters=a.iters, wall_s=dt,
+    out = dict(side=a.side, instances=a.instances, iters=a.iters, graphs=not a.no_graphs, wall_s=dt,
                voxel_iterations_per_s=a.instances * a.iters * n / dt)
     if a.time_kernels and st.p_launches:
         pm = (st.p_ms + st.u_ms) / st.p_launches

@@ -333,50 +333,106 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     int n_groups_active = ngroups;
     int listed = ngroups;   // groups in the current work list
     const dim3 block(kBX, kBY, 1);
+
+    // one iteration's launches on stream `s`: the flow sweeps of the four
+    // work-list segments, the label sweeps, and on check iterations the
+    // residual check; returns the number of launches
+    auto enqueue_iteration = [&](cudaStream_t s, bool check, bool time_it) -> int {
+        int n = 0;
+        if (time_it) cudaEventRecord(e0, s);
+        const int n4 = seg[2], n1 = seg[4] - seg[2];
+        if (seg[1] > seg[0])
+            bt_flow_kernel<true><<<seg[1] - seg[0], block, 0, s>>>(dwork + seg[0], dvols, dgroups, dmask);
+        if (seg[2] > seg[1])
+            bt_flow_kernel<false><<<seg[2] - seg[1], block, 0, s>>>(dwork + seg[1], dvols, dgroups, dmask);
+        if (seg[3] > seg[2])
+            bt1_flow_kernel<kAlphaArray><<<seg[3] - seg[2], block, 0, s>>>(dwork + seg[2], dvols, dgroups, dmask);
+        if (seg[4] > seg[3])
+            bt1_flow_kernel<kAlphaFromGrad2><<<seg[4] - seg[3], block, 0, s>>>(dwork + seg[3], dvols, dgroups,
+                                                                            dmask);
+        if (time_it) cudaEventRecord(e1, s);
+        if (n4 > 0) {
+            if (check) bt_label_kernel<true><<<n4, block, 0, s>>>(dwork, dvols, dgroups, dmask, dpart);
+            else bt_label_kernel<false><<<n4, block, 0, s>>>(dwork, dvols, dgroups, dmask, dpart);
+        }
+        if (n1 > 0) {
+            if (check) bt1_label_kernel<true><<<n1, block, 0, s>>>(dwork + seg[2], dvols, dgroups, dmask, dpart);
+            else bt1_label_kernel<false><<<n1, block, 0, s>>>(dwork + seg[2], dvols, dgroups, dmask, dpart);
+        }
+        if (time_it) cudaEventRecord(e2, s);
+        for (int k = 0; k < 4; ++k) n += seg[k + 1] > seg[k];
+        n += (n4 > 0) + (n1 > 0);
+        if (check) {
+            bt_check_kernel<<<ninst, 256, 0, s>>>(dvols, dgroups, dinsts, dctrl, dmask, dpart, params->error_bound,
+                                                  update, nullptr);
+            ++n;
+        }
+        return n;
+    };
+
+    // Full chunks (chunk iterations starting at a multiple of `update`, so
+    // the check pattern is the same in every one) are captured once per work
+    // list into a CUDA graph on a private stream and replayed on `st`; the
+    // last partial chunk and timed solves launch directly.
+    const bool use_graph = !timing && !(stats && (stats->flags & M16_BATCH_NO_GRAPH));
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int graph_launches = 0;
+    auto drop_graph = [&]() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        gexec = nullptr;
+        graph = nullptr;
+    };
+    auto release = [&]() {
+        drop_graph();
+        if (cap) cudaStreamDestroy(cap);
+        cap = nullptr;
+        if (timing) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            cudaEventDestroy(e2);
+        }
+    };
+#define M16_BT_TRY(expr)                                           \
+    do {                                                           \
+        cudaError_t e__ = (expr);                                  \
+        if (e__ != cudaSuccess) { release(); return M16_ERR_CUDA; } \
+    } while (0)
+    if (use_graph) M16_BT_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+
     while (it < params->num_iter && n_groups_active > 0 && !work.empty()) {
         const int end = std::min(params->num_iter, it + chunk);
-        for (; it < end; ++it) {
-            if (timing) cudaEventRecord(e0, st);
-            const bool check = (it % update) == 0;
-            const int n4 = seg[2], n1 = seg[4] - seg[2];
-            if (seg[1] > seg[0])
-                bt_flow_kernel<true><<<seg[1] - seg[0], block, 0, st>>>(dwork + seg[0], dvols, dgroups, dmask);
-            if (seg[2] > seg[1])
-                bt_flow_kernel<false><<<seg[2] - seg[1], block, 0, st>>>(dwork + seg[1], dvols, dgroups, dmask);
-            if (seg[3] > seg[2])
-                bt1_flow_kernel<kAlphaArray><<<seg[3] - seg[2], block, 0, st>>>(dwork + seg[2], dvols, dgroups, dmask);
-            if (seg[4] > seg[3])
-                bt1_flow_kernel<kAlphaFromGrad2><<<seg[4] - seg[3], block, 0, st>>>(dwork + seg[3], dvols, dgroups,
-                                                                                 dmask);
-            if (timing) cudaEventRecord(e1, st);
-            if (n4 > 0) {
-                if (check) bt_label_kernel<true><<<n4, block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
-                else bt_label_kernel<false><<<n4, block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
+        if (use_graph && end - it == chunk && it % update == 0) {
+            if (!gexec) {
+                M16_BT_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+                graph_launches = 0;
+                for (int k = 0; k < chunk; ++k) graph_launches += enqueue_iteration(cap, (k % update) == 0, false);
+                const cudaError_t ce = cudaStreamEndCapture(cap, &graph);
+                if (ce != cudaSuccess) { release(); return M16_ERR_CUDA; }
+                M16_BT_TRY(cudaGraphInstantiate(&gexec, graph, 0));
             }
-            if (n1 > 0) {
-                if (check) bt1_label_kernel<true><<<n1, block, 0, st>>>(dwork + seg[2], dvols, dgroups, dmask, dpart);
-                else bt1_label_kernel<false><<<n1, block, 0, st>>>(dwork + seg[2], dvols, dgroups, dmask, dpart);
-            }
-            if (timing) {
-                cudaEventRecord(e2, st);
-                M16_CUDA_TRY(cudaEventSynchronize(e2));
-                float a = 0.f, b = 0.f;
-                cudaEventElapsedTime(&a, e0, e1);
-                cudaEventElapsedTime(&b, e1, e2);
-                p_ms += a; ++p_n;
-                u_ms += b; ++u_n;
-            }
-            for (int k = 0; k < 4; ++k) launches += seg[k + 1] > seg[k];
-            launches += (n4 > 0) + (n1 > 0);
-            if (check) {
-                bt_check_kernel<<<ninst, 256, 0, st>>>(dvols, dgroups, dinsts, dctrl, dmask, dpart,
-                                                       params->error_bound, update, nullptr);
-                ++launches;
+            M16_BT_TRY(cudaGraphLaunch(gexec, st));
+            launches += graph_launches;
+            it = end;
+        } else {
+            for (; it < end; ++it) {
+                const bool check = (it % update) == 0;
+                launches += enqueue_iteration(st, check, timing);
+                if (timing) {
+                    M16_BT_TRY(cudaEventSynchronize(e2));
+                    float a = 0.f, b = 0.f;
+                    cudaEventElapsedTime(&a, e0, e1);
+                    cudaEventElapsedTime(&b, e1, e2);
+                    p_ms += a; ++p_n;
+                    u_ms += b; ++u_n;
+                }
             }
         }
-        M16_CUDA_TRY(cudaGetLastError());
-        M16_CUDA_TRY(cudaMemcpyAsync(hmask.data(), dmask, sizeof(unsigned) * ngroups, cudaMemcpyDeviceToHost, st));
-        M16_CUDA_TRY(cudaStreamSynchronize(st));
+        M16_BT_TRY(cudaGetLastError());
+        M16_BT_TRY(cudaMemcpyAsync(hmask.data(), dmask, sizeof(unsigned) * ngroups, cudaMemcpyDeviceToHost, st));
+        M16_BT_TRY(cudaStreamSynchronize(st));
         n_groups_active = 0;
         for (int g = 0; g < ngroups; ++g) {
             gactive[g] = hmask[g] != kAllLanes;
@@ -386,14 +442,12 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         if (n_groups_active > 0 && n_groups_active * 4 <= listed * 3) {
             build_work(work);
             listed = n_groups_active;
-            M16_CUDA_TRY(cudaMemcpyAsync(dwork, work.data(), sizeof(int2) * work.size(), cudaMemcpyHostToDevice, st));
+            M16_BT_TRY(cudaMemcpyAsync(dwork, work.data(), sizeof(int2) * work.size(), cudaMemcpyHostToDevice, st));
+            drop_graph();   // the segments changed: capture again
         }
     }
-    if (timing) {
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        cudaEventDestroy(e2);
-    }
+    release();
+#undef M16_BT_TRY
     for (int i = 0; i < ninst; ++i) {
         const int64_t n = hv[inst[i].volume].n;
         const int blocks = (int)std::min<int64_t>(kMaxBlocks, div_up(n, 256));

@@ -62,9 +62,20 @@ __global__ void gvf_init_kernel(const float *__restrict__ v3, const float *__res
     }
 }
 
-// gvfDelta + gvfUpdate (+ magDelta partial sums), gvf.cl:44-99, 162-202
+// gvfDelta + gvfUpdate (+ magDelta partial sums), gvf.cl:44-99, 162-202.
+// Each thread walks a z-column chunk; the loads of kGvfZB slices (the next
+// slice, the four in-plane neighbours and v) are issued together before any
+// of them is used, so each thread keeps several slices of loads in flight.
+#ifndef M16_GVF_ZB
+#define M16_GVF_ZB 2
+#endif
+#ifndef M16_GVF_MINB
+#define M16_GVF_MINB 1
+#endif
+constexpr int kGvfZB = M16_GVF_ZB;
+
 template <bool RESP, bool CHECK>
-__global__ void __launch_bounds__(kBX * kBY) gvf_sweep_kernel(GvfArgs a)
+__global__ void __launch_bounds__(kBX * kBY, M16_GVF_MINB) gvf_sweep_kernel(GvfArgs a)
 {
     __shared__ float red[32];
     if (__ldcg(&a.ctrl->stopped)) return;
@@ -81,42 +92,60 @@ __global__ void __launch_bounds__(kBX * kBY) gvf_sweep_kernel(GvfArgs a)
         const int64_t xb = a.d2 > 1 ? (x > 0 ? -1 : 1) : 0;
         const int64_t xa = a.d2 > 1 ? (x < a.d2 - 1 ? 1 : -1) : 0;
         int64_t i = ((int64_t)z0 * a.d1 + y) * a.d2 + x;
-        // carried along z: previous and current slice
         auto ld3 = [&](int64_t j, float &p, float &q, float &s) {
             p = __ldg(a.gi0 + j); q = __ldg(a.gi1 + j); s = __ldg(a.gi2 + j);
         };
+        // carried along z: previous and current slice
         float c0, c1, c2, p0, p1, p2;
         ld3(i, c0, c1, c2);
         if (a.d0 == 1) { p0 = c0; p1 = c1; p2 = c2; }
         else if (z0 > 0) ld3(i - s0, p0, p1, p2);
         else ld3(i + s0, p0, p1, p2);   // mirror at z = 0
-        for (int z = z0; z < z1; ++z, i += s0) {
-            float n0, n1, n2;   // z + 1 (mirror at the last slice)
-            if (a.d0 == 1) { n0 = c0; n1 = c1; n2 = c2; }
-            else if (z < a.d0 - 1) ld3(i + s0, n0, n1, n2);
-            else { n0 = p0; n1 = p1; n2 = p2; }
-            float yb0, yb1, yb2, ya0, ya1, ya2, xb0, xb1, xb2, xa0, xa1, xa2;
-            ld3(i + yb, yb0, yb1, yb2);
-            ld3(i + ya, ya0, ya1, ya2);
-            ld3(i + xb, xb0, xb1, xb2);
-            ld3(i + xa, xa0, xa1, xa2);
-            const float l0 = ((p0 + n0 - 2.f * c0) * a.rss0 + (yb0 + ya0 - 2.f * c0) * a.rss1) +
-                             (xb0 + xa0 - 2.f * c0) * a.rss2;
-            const float l1 = ((p1 + n1 - 2.f * c1) * a.rss0 + (yb1 + ya1 - 2.f * c1) * a.rss1) +
-                             (xb1 + xa1 - 2.f * c1) * a.rss2;
-            const float l2 = ((p2 + n2 - 2.f * c2) * a.rss0 + (yb2 + ya2 - 2.f * c2) * a.rss1) +
-                             (xb2 + xa2 - 2.f * c2) * a.rss2;
-            const float w0 = __ldg(a.v0 + i), w1 = __ldg(a.v1 + i), w2 = __ldg(a.v2 + i);
-            const float r = RESP ? __ldg(a.r + i) : w0 * w0 + w1 * w1 + w2 * w2;
-            const float e0 = r * (c0 - w0) - a.mu * l0;
-            const float e1 = r * (c1 - w1) - a.mu * l1;
-            const float e2 = r * (c2 - w2) - a.mu * l2;
-            a.go0[i] = c0 - a.dt * e0;
-            a.go1[i] = c1 - a.dt * e1;
-            a.go2[i] = c2 - a.dt * e2;
-            if (CHECK) acc += sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
-            p0 = c0; p1 = c1; p2 = c2;
-            c0 = n0; c1 = n1; c2 = n2;
+        for (int zb = z0; zb < z1; zb += kGvfZB, i += kGvfZB * s0) {
+            float nx[kGvfZB][3], nyb[kGvfZB][3], nya[kGvfZB][3], nxb[kGvfZB][3], nxa[kGvfZB][3], w[kGvfZB][3],
+                rr[kGvfZB];
+#pragma unroll
+            for (int k = 0; k < kGvfZB; ++k) {
+                const int z = zb + k;
+                if (z < z1) {
+                    const int64_t j = i + k * s0;
+                    if (z < a.d0 - 1) ld3(j + s0, nx[k][0], nx[k][1], nx[k][2]);   // z + 1
+                    ld3(j + yb, nyb[k][0], nyb[k][1], nyb[k][2]);
+                    ld3(j + ya, nya[k][0], nya[k][1], nya[k][2]);
+                    ld3(j + xb, nxb[k][0], nxb[k][1], nxb[k][2]);
+                    ld3(j + xa, nxa[k][0], nxa[k][1], nxa[k][2]);
+                    w[k][0] = __ldg(a.v0 + j); w[k][1] = __ldg(a.v1 + j); w[k][2] = __ldg(a.v2 + j);
+                    if (RESP) rr[k] = __ldg(a.r + j);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kGvfZB; ++k) {
+                const int z = zb + k;
+                if (z < z1) {
+                    const int64_t j = i + k * s0;
+                    float n0, n1, n2;   // z + 1 (mirror at the last slice)
+                    if (a.d0 == 1) { n0 = c0; n1 = c1; n2 = c2; }
+                    else if (z < a.d0 - 1) { n0 = nx[k][0]; n1 = nx[k][1]; n2 = nx[k][2]; }
+                    else { n0 = p0; n1 = p1; n2 = p2; }
+                    const float l0 = ((p0 + n0 - 2.f * c0) * a.rss0 + (nyb[k][0] + nya[k][0] - 2.f * c0) * a.rss1) +
+                                     (nxb[k][0] + nxa[k][0] - 2.f * c0) * a.rss2;
+                    const float l1 = ((p1 + n1 - 2.f * c1) * a.rss0 + (nyb[k][1] + nya[k][1] - 2.f * c1) * a.rss1) +
+                                     (nxb[k][1] + nxa[k][1] - 2.f * c1) * a.rss2;
+                    const float l2 = ((p2 + n2 - 2.f * c2) * a.rss0 + (nyb[k][2] + nya[k][2] - 2.f * c2) * a.rss1) +
+                                     (nxb[k][2] + nxa[k][2] - 2.f * c2) * a.rss2;
+                    const float w0 = w[k][0], w1 = w[k][1], w2 = w[k][2];
+                    const float r = RESP ? rr[k] : w0 * w0 + w1 * w1 + w2 * w2;
+                    const float e0 = r * (c0 - w0) - a.mu * l0;
+                    const float e1 = r * (c1 - w1) - a.mu * l1;
+                    const float e2 = r * (c2 - w2) - a.mu * l2;
+                    a.go0[j] = c0 - a.dt * e0;
+                    a.go1[j] = c1 - a.dt * e1;
+                    a.go2[j] = c2 - a.dt * e2;
+                    if (CHECK) acc += sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
+                    p0 = c0; p1 = c1; p2 = c2;
+                    c0 = n0; c1 = n1; c2 = n2;
+                }
+            }
         }
     }
     if (CHECK) {
@@ -179,7 +208,9 @@ inline int gvf_zc(int d0, int d1, int d2)
 {
     const int64_t cols = div_up(d2, kBX) * div_up(d1, kBY);
     int64_t zc = (int64_t)d0 * cols / (8 * kSMs);
-    return (int)std::max<int64_t>(1, std::min<int64_t>(16, zc));
+    zc = std::max<int64_t>(1, std::min<int64_t>(16, zc));
+    if (zc >= kGvfZB) zc = zc / kGvfZB * kGvfZB;   // whole load batches
+    return (int)zc;
 }
 
 inline GvfLayout gvf_layout(int d0, int d1, int d2, int has_response, int mags_cap)

@@ -106,3 +106,26 @@ def test_groups_of_four_with_padding_and_mixed_eigenvalues():
         u, it = _plain(vols[0], inst, 90, 30, -1.0)
         assert its[k] == it == 90
         assert np.max(np.abs(us[k] - u)) <= U_TOL, k
+
+
+def test_graph_replay_equals_direct_launches():
+    """Whole check intervals replayed as CUDA graphs (re-captured when
+    finished groups leave the work list) give the same bits as launching
+    every iteration directly."""
+    from miccai2016_gb300.batched import BatchedCut
+    vols = [_volume(6, (28, 24, 40)), _volume(7, (16, 16, 16))]
+    insts = [dict(volume=v, weighting=w, decay=d, eigs=e) for v in (0, 1) for w in (0.01, 0.1, 1.0)
+             for d in (1.0, 30.0) for e in (ATV, TV)]
+    p = BatchedCut.CutParameters()
+    p.num_iter, p.update, p.error_bound = 1500, 10, 2e-3
+    out = []
+    for graphs in (True, False):
+        b = BatchedCut(p)
+        dv = [b.prepare_volume(v["img"], v["quats"], v["cs"], v["ct"], grad2=v["grad2"]) for v in vols]
+        us = b.solve(dv, insts, graphs=graphs)
+        out.append(([u.cpu().numpy() for u in us], b.last_iterations.copy(), b.last_residuals.copy()))
+    (ua, ia, ra), (ub, ib, rb) = out
+    assert len(set(ia.tolist())) > 2               # groups finish at different checks
+    assert np.array_equal(ia, ib) and np.array_equal(ra, rb, equal_nan=True)
+    for a, b_ in zip(ua, ub):
+        assert np.array_equal(a.view(np.uint32), b_.view(np.uint32))
