@@ -17,6 +17,11 @@ iterations (residual checked every 30).  One step = one solve.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun every rank runs its own replica (the solves are independent).
+
+Other workloads (one JSON line each, not the headline):
+  --workload stages128|stages256   every pre-cut pipeline stage, timed per call
+  --workload ragged                the ragged batch (4 volume shapes x noise levels)
+  --workload plain64|plain128      the headline solve at smaller sizes
 """
 from __future__ import annotations
 
@@ -224,6 +229,7 @@ def run_ours(args, cfg):
         torch.cuda.set_device(0)
     from miccai2016_gb300 import _native as N
     from miccai2016_gb300 import phantom as P
+    from miccai2016_gb300 import replicas
     from miccai2016_gb300.continuous_cut_anisotropic_gpu import CmfCutQAnisotropicGpu
 
     L = N.lib()
@@ -285,9 +291,7 @@ def run_ours(args, cfg):
     torch.cuda.synchronize()
     clocks = sampler.stop() if sampler else None
     if dist:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = replicas.max_over_ranks(ms, device=dev)
     ms_per_step = ms / args.steps
     value = world * args.steps / (ms / 1000.0)
 
@@ -316,9 +320,7 @@ def run_ours(args, cfg):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if dist:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = replicas.max_over_ranks(e2e_s, device=dev)
     e2e_value = world * e2e_steps / e2e_s
     dice = float(P.fast_dice(out.numpy(), inp["truth"]))
 
@@ -364,7 +366,7 @@ def run_ours(args, cfg):
                              "sample": sample},
             "clocks": clocks, "dice_fast": dice,
             "voxel_iterations_per_s": value * n * cfg["num_iter"]}
-    if cfg["name"] == "plain256":   # the default workload also reports the batched grid search and serving
+    if cfg["name"] == "plain256" and not args.no_batched:   # the default workload also reports the grid search and serving
         line["batched"] = run_batched_grid()
         if args.served_requests > 0:
             from miccai2016_gb300.serving import served_vs_plain
@@ -381,6 +383,7 @@ def run_batched_grid(plain_sample=17):
     import torch
     from miccai2016_gb300 import phantom as P, pipeline
     from miccai2016_gb300.batched import BatchedCut
+    from miccai2016_gb300.capacities import fast_dice
     from miccai2016_gb300.continuous_cut_anisotropic_gpu import CmfCutQAnisotropicGpu
     cfg = P.CONFIG_GRID_128
     noisy, truth = P.helix_phantom(cfg["shape"], cfg["tube_radius"], cfg["helix_radius"], cfg["pitch"],
@@ -409,8 +412,7 @@ def run_batched_grid(plain_sample=17):
     batched_s = e0.elapsed_time(e1) / 1000.0
     iters = bc.last_iterations.copy()
     truth_d = torch.from_numpy(truth).cuda()
-    tsum = float(truth_d.sum())
-    dice_b = np.array([float(2 * ((u >= 0.5) * truth_d).sum() / ((u >= 0.5).sum() + tsum)) for u in us])
+    dice_b = np.asarray(fast_dice(us, truth_d))
     del us
     best = int(np.argmax(dice_b))
     # plain path on a sample: the decays of the best weighting (17 instances)
@@ -420,8 +422,9 @@ def run_batched_grid(plain_sample=17):
     cp.num_iter, cp.update, cp.error_bound = cfg["num_iter"], cfg["update"], cfg["error_bound"]
     cutter = CmfCutQAnisotropicGpu(cp)
     d_img, d_q = vol["img"], vol["quats"]
-    alphas = [torch.from_numpy(P.nonterminal_weights(cut["grad2_f64"], grid[k][0], grid[k][1]).astype(np.float32))
-              .cuda() for k in sample]
+    # alpha = w * exp(-|grad I|^2 / decay^2) in float32, as the batched flow sweep evaluates it
+    alphas = [(torch.exp(vol["grad2"] * np.float32(-1.0 / grid[k][1] ** 2)) * np.float32(grid[k][0])).contiguous()
+              for k in sample]
     cutter.execute(d_img, d_q, P.ATV_EIGS, alphas[0], vol["cs"], vol["ct"], verbose=False)   # warm-up
     torch.cuda.synchronize()
     e0.record(stream)
@@ -433,7 +436,7 @@ def run_batched_grid(plain_sample=17):
     e1.record(stream)
     torch.cuda.synchronize()
     plain_s = e0.elapsed_time(e1) / 1000.0
-    dice_p = np.array([float(2 * ((u >= 0.5) * truth_d).sum() / ((u >= 0.5).sum() + tsum)) for u in plain_u])
+    dice_p = np.asarray(fast_dice(plain_u, truth_d))
     n_vox = int(np.prod(cfg["shape"]))
     vox_it = float(np.sum(iters)) * n_vox
     batched_rate = len(insts) / batched_s
@@ -454,6 +457,242 @@ def run_batched_grid(plain_sample=17):
             "ridge_points": cut["ridge_points"]}
 
 
+RAGGED_SHAPES = [(96, 96, 96), (128, 128, 192), (160, 160, 160), (224, 224, 160)]
+
+
+def run_ragged(args):
+    """Ragged batch: noise levels linspace(0.1, 1.5, 15)[::step] x the four
+    volume shapes, each a helix phantom with its own helix radius (0.2-0.3 of
+    the smallest extent) and tube radius (2-6 voxels) drawn from a seeded
+    RandomState.  Every volume runs the GPU pipeline (Frangi at sigma 1-3,
+    sign adjustment, GVF, completion, capacities); then all cuts run as one
+    m16_batch_solve (ATV, weighting 10^-1.25, decay 10^1.5, stop at residual
+    1e-4, update 30, at most 3000 iterations) against the same cuts solved one
+    by one with CmfCutQAnisotropicGpu.execute() on device-resident inputs.
+    Prints one JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    from miccai2016_gb300 import phantom as P, pipeline
+    from miccai2016_gb300.batched import BatchedCut
+    from miccai2016_gb300.capacities import fast_dice
+    from miccai2016_gb300.continuous_cut_anisotropic_gpu import CmfCutQAnisotropicGpu
+    sigmas = np.linspace(0.1, 1.5, 15)[::max(1, args.ragged_step)]
+    rng = np.random.RandomState(2016)
+    w, d = 10 ** -1.25, 10 ** 1.5
+    vols, truths, prep = [], [], []
+    bp = BatchedCut.CutParameters()
+    bp.num_iter, bp.update, bp.error_bound = 3000, 30, 1e-4
+    bc = BatchedCut(bp)
+    t_prep = time.perf_counter()
+    for sg in sigmas:
+        for shape in RAGGED_SHAPES:
+            hr = float(rng.uniform(0.2, 0.3) * min(shape))
+            tr = float(rng.uniform(2.0, 6.0))
+            noisy, truth = P.helix_phantom(shape, tr, hr, 2.5 * hr, float(sg), seed=int(rng.randint(1 << 30)))
+            t0 = time.perf_counter()
+            cut, _ = pipeline.prepare_cut_inputs(noisy, float(sg), scales=(1, 3, 3))
+            prep.append(time.perf_counter() - t0)
+            vols.append(bc.prepare_volume(noisy, cut["quats"], cut["fgw"], cut["bgw"], grad2=cut["grad2"]))
+            truths.append(torch.from_numpy(truth).cuda())
+    t_prep = time.perf_counter() - t_prep
+    insts = [dict(volume=k, weighting=w, decay=d, eigs=P.ATV_EIGS) for k in range(len(vols))]
+    wp = BatchedCut.CutParameters()
+    wp.num_iter, wp.update, wp.error_bound = 60, 30, -1.0
+    BatchedCut(wp).solve(vols[:2], insts[:2])   # loads the kernels
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    us = bc.solve(vols, insts)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_s = e0.elapsed_time(e1) / 1000.0
+    iters_b = bc.last_iterations.copy()
+    dice_b = np.asarray([fast_dice(u, t) for u, t in zip(us, truths)])
+    del us
+    cp = CmfCutQAnisotropicGpu.CutParameters()
+    cp.num_iter, cp.update, cp.error_bound = 3000, 30, 1e-4
+    cutter = CmfCutQAnisotropicGpu(cp)
+    alphas = [(torch.exp(v["grad2"] * np.float32(-1.0 / d ** 2)) * np.float32(w)).contiguous() for v in vols]
+    cutter.execute(vols[0]["img"], vols[0]["quats"], P.ATV_EIGS, alphas[0], vols[0]["cs"], vols[0]["ct"],
+                   verbose=False)
+    torch.cuda.synchronize()
+    plain_s = 0.0
+    dice_p, iters_p = [], []
+    for v, a, t in zip(vols, alphas, truths):
+        e0.record(stream)
+        u = cutter.execute(v["img"], v["quats"], P.ATV_EIGS, a, v["cs"], v["ct"], verbose=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain_s += e0.elapsed_time(e1) / 1000.0
+        iters_p.append(cutter.last_iterations)
+        dice_p.append(fast_dice(u, t))
+    n = len(vols)
+    vox = np.array([int(np.prod(v["shape"])) for v in vols], np.float64)
+    line = {"impl": "ours", "workload": "ragged batch: %d noise levels x shapes %s, helix phantoms, GPU pipeline "
+                                        "per volume, ATV cut w=10^-1.25 decay=10^1.5, stop at residual 1e-4" % (
+                                            len(sigmas), RAGGED_SHAPES),
+            "volumes": n, "batched_solves_per_s": n / batched_s, "plain_solves_per_s": n / plain_s,
+            "speedup_vs_plain": plain_s / batched_s, "batched_s": batched_s, "plain_s": plain_s,
+            "voxel_iterations_per_s_batched": float(np.sum(vox * iters_b)) / batched_s,
+            "iterations": {"min": int(iters_b.min()), "median": float(np.median(iters_b)), "max": int(iters_b.max())},
+            "iteration_diff_vs_plain": int(np.max(np.abs(iters_b - np.asarray(iters_p)))),
+            "max_dice_diff_vs_plain": float(np.max(np.abs(dice_b - np.asarray(dice_p)))),
+            "dice_fast": {"min": float(dice_b.min()), "median": float(np.median(dice_b)), "max": float(dice_b.max())},
+            "preparation_s_per_volume": {"median": float(np.median(prep)), "max": float(np.max(prep))},
+            "preparation_total_s": t_prep}
+    print(json.dumps(line), flush=True)
+
+
+STAGE_BYTES = {
+    # algorithmic (compulsory) bytes per unit of each pipeline stage, fp32
+    "frangi": 72,          # per voxel-scale: image 4 read, Hessian 24 written + read, val 4 + 4, quat 12
+    "detect_ridges": 20,   # per voxel: response 4 + quaternion 12 read, ridge 4 written
+    "extract_main_dirs": 24,        # per voxel: quaternion 12 read, direction 12 written
+    "gvf": 40,             # per voxel-iteration: g 12, v 12, r 4 read; g 12 written
+    "complete_transformations": 24,  # per voxel: direction 12 read, quaternion 12 written
+}
+STAGES = ["frangi", "detect_ridges", "extract_main_dirs", "adjust_nonridge_signs", "gvf", "complete_transformations"]
+
+
+def run_stages(args, cfg):
+    """The plain pipeline's stages before the cut, one C-ABI call each on
+    device-resident inputs of the workload's helix phantom, timed with CUDA
+    events over --steps calls after --warmup calls: Frangi at sigma 1, 2, 3
+    (c from the Hessian norm), ridge candidates, main directions, the indexed
+    nearest-ridge sign flip (its ridge list from the host steps of
+    AdvancedAdjuster), GVF (100 iterations, mu 0.2) and the completion to
+    quaternions.  --stages picks a subset (the others run untimed where a
+    later stage needs their output).  Prints one JSON line."""
+    import contextlib
+    import io
+
+    import torch
+    torch.cuda.set_device(0)
+    from miccai2016_gb300 import _native as N
+    from miccai2016_gb300 import phantom as P
+    from miccai2016_gb300.adjust_directions import AdvancedAdjuster
+    from miccai2016_gb300.gradient_vector_flow import time_step_for
+    from miccai2016_gb300.qfrangi_gpu import pack_taps, scales_in_voxels
+
+    L = N.lib()
+    shape = tuple(cfg["shape"])
+    d0, d1, d2 = shape
+    n = d0 * d1 * d2
+    noisy, _ = P.helix_phantom(shape, cfg["tube_radius"], cfg["helix_radius"], cfg["pitch"], cfg["sigma"],
+                               cfg["seed"])
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream()
+    sp = N.stream_ptr()
+    peak, peak_kind = _peaks()
+    img = torch.from_numpy(noisy).to(dev)
+    wanted = set(args.stages.split(",")) if args.stages else set(STAGES)
+    unknown = wanted - set(STAGES)
+    if unknown:
+        raise SystemExit("unknown stages %s" % sorted(unknown))
+
+    def timed(fn, steps=args.steps, warmup=args.warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    out = {}
+
+    def stage(name, fn, units, unit_name, bytes_per_unit=None, extra=None):
+        """Times fn when the stage is wanted, else runs it once."""
+        if name not in wanted:
+            fn()
+            return
+        ms = timed(fn)
+        ent = {"ms": ms, unit_name: units, "units_per_s": units / (ms * 1e-3)}
+        if bytes_per_unit is not None:
+            gbs = bytes_per_unit * units / (ms * 1e-3) / 1e9
+            ent.update({"bytes_per_unit": bytes_per_unit, "GB/s": gbs, "frac": gbs / peak})
+        if extra:
+            ent.update(extra(ms) if callable(extra) else extra)
+        out[name] = ent
+
+    # Frangi, scales 1..3 (3 scales), c = None
+    sig = scales_in_voxels((1, 3, 3), np.ones(3))
+    taps, radius = pack_taps(sig)
+    m = sig.shape[0]
+    val = torch.empty(shape, dtype=torch.float32, device=dev)
+    quat = torch.empty(shape + (3,), dtype=torch.float32, device=dev)
+    ws = N.workspace(L.m16_frangi_workspace_bytes(d0, d1, d2, m))
+    stage("frangi", lambda: N.check("m16_frangi", L.m16_frangi(
+        N.ptr(img), d0, d1, d2, m, taps.ctypes.data_as(ctypes.c_void_p), radius.ctypes.data_as(ctypes.c_void_p),
+        0.5, 0.5, -1.0, 1, N.ptr(val), N.ptr(quat), None, N.ptr(ws), ws.numel(), sp)),
+        n * m, "voxel_scales", STAGE_BYTES["frangi"], {"scales": [1, 2, 3], "c": "half the max Hessian norm per scale"})
+    del ws
+    vmin, vmax = float(val.min()), float(val.max())
+    resp = ((val - vmin) / (vmax - vmin)).contiguous()
+
+    ridge = torch.empty(shape, dtype=torch.float32, device=dev)
+    stage("detect_ridges", lambda: N.check("m16_detect_ridges", L.m16_detect_ridges(
+        N.ptr(resp), N.ptr(quat), d0, d1, d2, 0.01, N.ptr(ridge), sp)), n, "voxels", STAGE_BYTES["detect_ridges"])
+    dirs = torch.empty_like(quat)
+    stage("extract_main_dirs", lambda: N.check("m16_extract_main_directions", L.m16_extract_main_directions(
+        N.ptr(quat), n, N.ptr(dirs), sp)), n, "voxels", STAGE_BYTES["extract_main_dirs"])
+
+    # the ridge list of the host steps (hysteresis, MST, cleaning), then the GPU sign flip
+    work = dirs.clone()
+    if "adjust_nonridge_signs" in wanted or "gvf" in wanted or "complete_transformations" in wanted:
+        t0 = time.perf_counter()
+        adj = AdvancedAdjuster(threshold=(0.01, 0.3), qeigs=quat.cpu().numpy(), response=resp.cpu().numpy(),
+                               voxel_size=(1, 1, 1), ridge_detection_only=True, clean_ridge=True)
+        with contextlib.redirect_stdout(io.StringIO()):
+            adj.execute(verbose=False)
+            adj._d_qeigs = quat.clone()
+            main_dirs = adj._qeigs_to_main_dirs()
+            coords, rdirs = adj._adjust_ridge_directions(adj.ridge, main_dirs)
+        host_s = time.perf_counter() - t0
+        R = int(len(coords))
+        d_coords = torch.from_numpy(np.ascontiguousarray(coords, np.uint16).view(np.int16)).to(dev)
+        d_rdirs = torch.from_numpy(np.ascontiguousarray(rdirs, np.float32)).to(dev)
+        sc = (ctypes.c_double * 3)(1.0, 1.0, 1.0)
+        nws = N.workspace(L.m16_adjust_nonridge_signs_workspace_bytes(d0, d1, d2, R))
+        stage("adjust_nonridge_signs", lambda: N.check("m16_adjust_nonridge_signs_indexed",
+                                                       L.m16_adjust_nonridge_signs_indexed(
+                                                           N.ptr(work), d0, d1, d2, N.ptr(d_coords), N.ptr(d_rdirs),
+                                                           R, sc, N.ptr(nws), nws.numel(), sp)),
+              n, "voxels", extra=lambda ms: {
+                  "ridge_points": R, "host_steps_s": host_s,
+                  "host_steps": "hysteresis, ridge MST and sign propagation, cleaning (numpy/scipy)",
+                  "kernel": "m16_adjust_nonridge_signs_indexed (cell index build + shell search)",
+                  "brute_force_equivalent_evaluations_per_s": n * R / (ms * 1e-3)})
+
+    # GVF of the sign-adjusted directions scaled by the response, 100 iterations
+    vf = (work * resp.unsqueeze(-1)).contiguous()
+    g = torch.empty_like(vf)
+    iters = int(cfg.get("gvf_iter", 100))
+    mu = float(cfg.get("gvf_mu", 0.2))
+    dt = float(time_step_for(np.ones(3), mu, 3))
+    cap = iters // 10 + 2
+    ws = N.workspace(L.m16_gvf_workspace_bytes(d0, d1, d2, 0, cap))
+    vs = (ctypes.c_double * 3)(1.0, 1.0, 1.0)
+    mags = (ctypes.c_double * cap)()
+    it, stp, nm = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+    stage("gvf", lambda: N.check("m16_gvf_run", L.m16_gvf_run(
+        N.ptr(vf), None, d0, d1, d2, vs, mu, dt, 0, iters, 10, 0.0, 0, N.ptr(g), ctypes.byref(it),
+        ctypes.byref(stp), mags, cap, ctypes.byref(nm), N.ptr(ws), ws.numel(), sp)), n * iters,
+        "voxel_iterations", STAGE_BYTES["gvf"], {"iterations": iters, "mu": mu})
+    del ws
+    q2 = torch.empty_like(g)
+    stage("complete_transformations", lambda: N.check("m16_complete_transformations", L.m16_complete_transformations(
+        N.ptr(g), n, N.ptr(q2), sp)), n, "voxels", STAGE_BYTES["complete_transformations"])
+    line = {"impl": "ours", "workload": "pipeline stages before the cut, %s helix phantom (noise sigma %g)" % (
+        "x".join(map(str, shape)), cfg["sigma"]), "steps": args.steps, "warmup": args.warmup,
+        "peak_gbs": peak, "peak_kind": peak_kind, "stages": out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -462,9 +701,21 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain256")
     ap.add_argument("--ref-iters", type=int, default=3, help="iterations per CPU-baseline sample")
+    ap.add_argument("--stages", default="",
+                    help="stages workloads: comma-separated subset of %s (default: all)" % ",".join(STAGES))
+    ap.add_argument("--ragged-step", type=int, default=1,
+                    help="ragged workload: every k-th of the 15 noise levels")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched grid search and the serving comparison of the default workload")
     ap.add_argument("--served-requests", type=int, default=96,
                     help="requests of the serving comparison (0 skips it)")
     args = ap.parse_args()
+    if args.workload == "ragged":
+        run_ragged(args)
+        return
+    if args.workload.startswith("stages"):
+        run_stages(args, _workload("plain" + args.workload[len("stages"):]))
+        return
     cfg = _workload(args.workload)
     if args.impl == "reference":
         run_reference(args, cfg)
