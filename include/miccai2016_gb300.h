@@ -111,11 +111,20 @@ typedef struct m16_solve_stats {
     double u_ms;           /* out: summed device time of the U launches (time_kernels only) */
     int32_t path;          /* in: M16_PATH_* -- how an iteration is launched */
     int32_t flags;         /* in: M16_BATCH_* options of m16_batch_solve (0 elsewhere) */
+    int32_t blocks_per_sm; /* out (m16_batch_solve): the sweeps' tile shape in use at the end, as the
+                              target blocks per SM its z-chunk was chosen for */
+    int32_t reserved;
 } m16_solve_stats;
 
 /* m16_solve_stats.flags: launch every iteration directly instead of replaying
  * CUDA graphs of whole check intervals (timed solves always launch directly). */
 #define M16_BATCH_NO_GRAPH 1
+/* m16_solve_stats.flags: use the default tile shape.  Without it the
+ * sweeps' tile shape is tuned: a batch of a shape not seen before in this
+ * process times the candidate shapes on its first check intervals (real
+ * iterations of the solve) and keeps the fastest, later batches of that shape
+ * reuse it.  Timed solves and batches too small to matter use the default. */
+#define M16_BATCH_NO_TUNE 2
 
 /* m16_maxflow_solve with counters; stats (host) may be NULL. */
 int m16_maxflow_solve_ex(const float *img, const float *quat3, const double *sqevals3,

@@ -54,12 +54,14 @@ PATH_DEFAULT, PATH_TWO_SWEEPS, PATH_FUSED = 0, 1, 2
 
 
 BATCH_NO_GRAPH = 1   # m16_solve_stats.flags
+BATCH_NO_TUNE = 2
 
 
 class SolveStats(ctypes.Structure):
     """m16_solve_stats (include/miccai2016_gb300.h)."""
     _fields_ = [("time_kernels", _i32), ("launches", _i32), ("p_launches", _i32), ("u_launches", _i32),
-                ("p_ms", _f64), ("u_ms", _f64), ("path", _i32), ("flags", _i32)]
+                ("p_ms", _f64), ("u_ms", _f64), ("path", _i32), ("flags", _i32),
+                ("blocks_per_sm", _i32), ("reserved", _i32)]
 
 
 class BatchVolume(ctypes.Structure):

@@ -90,19 +90,19 @@ struct InstDev {
     const float *alpha;
 };
 
-// z-slices per block: enough blocks for M16_BATCH_BLOCKS_PER_SM per SM over
-// the volume's groups (many short blocks keep the last wave short), at most 32
+// z-slices per block: enough blocks for `blocks_per_sm` (by default
+// M16_BATCH_BLOCKS_PER_SM) per SM over the volume's groups (many short blocks
+// keep the last wave short), at most 32
 #ifndef M16_BATCH_BLOCKS_PER_SM
 #define M16_BATCH_BLOCKS_PER_SM 16
 #endif
 #ifndef M16_BATCH_MINB
 #define M16_BATCH_MINB 3
 #endif
-inline int batch_zc(int d0, int d1, int d2, int ngroups_of_volume)
+inline int batch_zc(int d0, int d1, int d2, int ngroups_of_volume, int blocks_per_sm = M16_BATCH_BLOCKS_PER_SM)
 {
     const int64_t cols = div_up(d2, kBX) * div_up(d1, kBY);
-    int64_t zc = (int64_t)d0 * cols * std::max(ngroups_of_volume, 1) /
-                 ((int64_t)M16_BATCH_BLOCKS_PER_SM * kSMs);
+    int64_t zc = (int64_t)d0 * cols * std::max(ngroups_of_volume, 1) / ((int64_t)blocks_per_sm * kSMs);
     zc = std::max<int64_t>(1, std::min<int64_t>(32, zc));
     return (int)zc;
 }

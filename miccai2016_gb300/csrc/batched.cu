@@ -6,7 +6,9 @@
 #include <float.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <map>
+#include <mutex>
 #include <tuple>
 #include <vector>
 
@@ -98,6 +100,16 @@ struct BatchLayout {
 
 constexpr int kMaxBlocks = 4 * kSMs;
 
+// Autotuner of the sweeps' tile shape: the z-chunk of a (32 x 8 x zc) tile
+// follows from a target number of blocks per SM; the candidates are timed on
+// one check interval each of the solve itself and the fastest is kept for the
+// rest of it and for later batches of the same shape (a process-wide cache).
+constexpr int kTuneBps[3] = {8, 16, 32};
+constexpr int kTuneMinItems = kSMs;   // smaller work lists are launch-bound: keep the default
+
+std::mutex g_tune_mu;
+std::map<std::vector<int64_t>, int> g_tuned;   // batch shape -> blocks per SM
+
 inline BatchLayout batch_layout(const m16_batch_volume *vols, int nvol, const m16_batch_instance *inst, int ninst,
                                 const Plan &P)
 {
@@ -109,7 +121,9 @@ inline BatchLayout batch_layout(const m16_batch_volume *vols, int nvol, const m1
         const int64_t n = (int64_t)vols[v].d0 * vols[v].d1 * vols[v].d2;
         L.q4.push_back(take(n * 16));
         L.maxpart.push_back(take(kMaxBlocks * 4));
-        const int zc = batch_zc(vols[v].d0, vols[v].d1, vols[v].d2, P.ngroups_of_vol[v]);
+        // sized for the candidate with the most (smallest) tiles
+        int zc = 32;
+        for (int c : kTuneBps) zc = std::min(zc, batch_zc(vols[v].d0, vols[v].d1, vols[v].d2, P.ngroups_of_vol[v], c));
         tiles[v] = div_up(vols[v].d2, kBX) * div_up(vols[v].d1, kBY) * div_up(vols[v].d0, zc);
     }
     L.total_blocks = 0;
@@ -192,7 +206,7 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         const m16_batch_volume &V = vols[v];
         VolDev &d = hv[v];
         d.d0 = V.d0; d.d1 = V.d1; d.d2 = V.d2;
-        d.zc = batch_zc(V.d0, V.d1, V.d2, P.ngroups_of_vol[v]);
+        d.zc = batch_zc(V.d0, V.d1, V.d2, P.ngroups_of_vol[v]);   // set again by configure()
         d.tx = (int)div_up(V.d2, kBX); d.ty = (int)div_up(V.d1, kBY); d.tz = (int)div_up(V.d0, d.zc);
         const double *sc = V.scaling;
         const double smin = fmin(sc[0], fmin(sc[1], sc[2]));
@@ -315,8 +329,56 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         seg[4] = (int)w.size();
     };
     std::vector<int2> work;
-    build_work(work);
-    M16_CUDA_TRY(cudaMemcpyAsync(dwork, work.data(), sizeof(int2) * work.size(), cudaMemcpyHostToDevice, st));
+
+    // tile shape: z-chunks for `bps` blocks per SM, the groups' partial-sum
+    // slots, the work list (the volumes' max / denominator fields written by
+    // the set-up kernels are left alone: only zc..tz are copied)
+    int cur_bps = 0;
+    auto configure = [&](int bps) -> cudaError_t {
+        for (int v = 0; v < nvol; ++v) {
+            VolDev &d = hv[v];
+            d.zc = batch_zc(d.d0, d.d1, d.d2, P.ngroups_of_vol[v], bps);
+            d.tz = (int)div_up(d.d0, d.zc);
+            cudaError_t e = cudaMemcpyAsync((char *)(dvols + v) + offsetof(VolDev, zc), &d.zc, 4 * sizeof(int),
+                                            cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+        int64_t off = 0;
+        for (int g = 0; g < ngroups; ++g) {
+            const VolDev &V = hv[hg[g].vol];
+            hg[g].part_off = off;
+            hg[g].nparts = V.tx * V.ty * V.tz;
+            off += hg[g].nparts;
+        }
+        cudaError_t e = cudaMemcpyAsync(dgroups, hg.data(), sizeof(GroupDev) * ngroups, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return e;
+        build_work(work);
+        cur_bps = bps;
+        // the host vectors must stay unchanged until the copies ran
+        e = cudaMemcpyAsync(dwork, work.data(), sizeof(int2) * work.size(), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return e;
+        return cudaStreamSynchronize(st);
+    };
+    std::vector<int64_t> tune_key;
+    for (int v = 0; v < nvol; ++v) {
+        tune_key.push_back(vols[v].d0); tune_key.push_back(vols[v].d1); tune_key.push_back(vols[v].d2);
+        tune_key.push_back(P.ngroups_of_vol[v]);
+    }
+    for (int g = 0; g < ngroups; ++g) tune_key.push_back(hg[g].lanes * 2 + hg[g].has_alpha);
+    tune_key.push_back(params->update);
+    int start_bps = M16_BATCH_BLOCKS_PER_SM;
+    bool tune = false;
+    if (!(stats && (stats->flags & M16_BATCH_NO_TUNE))) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto f = g_tuned.find(tune_key);
+        if (f != g_tuned.end()) start_bps = f->second;
+        else tune = true;
+    }
+    M16_CUDA_TRY(configure(start_bps));
+    const bool timed_solve = stats && stats->time_kernels;
+    if (timed_solve || (stats && (stats->flags & M16_BATCH_NO_TUNE)) || (int64_t)work.size() < kTuneMinItems ||
+        params->num_iter < 4 * params->update)
+        tune = false;
 
     const int update = params->update;
     const int chunk = update * std::max(1, 64 / update);
@@ -385,10 +447,13 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         gexec = nullptr;
         graph = nullptr;
     };
+    cudaEvent_t *tune_events[2] = {nullptr, nullptr};
     auto release = [&]() {
         drop_graph();
         if (cap) cudaStreamDestroy(cap);
         cap = nullptr;
+        for (cudaEvent_t *e : tune_events)
+            if (e && *e) { cudaEventDestroy(*e); *e = nullptr; }
         if (timing) {
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
@@ -402,9 +467,52 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     } while (0)
     if (use_graph) M16_BT_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
 
+    // tuning: check intervals [k update, (k + 1) update) run candidate k,
+    // timed from after their check iteration to their end
+    int tune_stage = tune ? 0 : -1;
+    double tune_ms[3] = {0.0, 0.0, 0.0};
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    tune_events[0] = &t0;
+    tune_events[1] = &t1;
+    if (tune) {
+        M16_BT_TRY(cudaEventCreate(&t0));
+        M16_BT_TRY(cudaEventCreate(&t1));
+        if (cur_bps != kTuneBps[0]) M16_BT_TRY(configure(kTuneBps[0]));
+    }
     while (it < params->num_iter && n_groups_active > 0 && !work.empty()) {
+        if (tune_stage >= 0) {
+            const int end = std::min(params->num_iter, it + update);
+            int64_t vox = 0;   // voxels of the active groups: the work this interval does
+            for (int g = 0; g < ngroups; ++g)
+                if (gactive[g]) vox += hv[hg[g].vol].n * hg[g].lanes;
+            for (; it < end; ++it) {
+                launches += enqueue_iteration(st, (it % update) == 0, false);
+                if (it % update == 0) M16_BT_TRY(cudaEventRecord(t0, st));
+            }
+            M16_BT_TRY(cudaEventRecord(t1, st));
+            M16_BT_TRY(cudaEventSynchronize(t1));
+            float ms = 0.f;
+            M16_BT_TRY(cudaEventElapsedTime(&ms, t0, t1));
+            tune_ms[tune_stage] = vox > 0 ? (double)ms / (double)vox : 0.0;
+            ++tune_stage;
+            if (tune_stage == 3) {
+                int best = 0;
+                for (int k = 1; k < 3; ++k)
+                    if (tune_ms[k] < tune_ms[best]) best = k;
+                {
+                    std::lock_guard<std::mutex> lk(g_tune_mu);
+                    g_tuned[tune_key] = kTuneBps[best];
+                }
+                tune_stage = -1;
+                if (cur_bps != kTuneBps[best]) M16_BT_TRY(configure(kTuneBps[best]));
+            } else {
+                M16_BT_TRY(configure(kTuneBps[tune_stage]));
+            }
+        }
         const int end = std::min(params->num_iter, it + chunk);
-        if (use_graph && end - it == chunk && it % update == 0) {
+        if (it >= params->num_iter) {
+            // tuning ran the last iterations
+        } else if (use_graph && end - it == chunk && it % update == 0) {
             if (!gexec) {
                 M16_BT_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
                 graph_launches = 0;
@@ -462,6 +570,7 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         if (residuals) residuals[i] = hctrl[i].resid;
     }
     if (stats) {
+        stats->blocks_per_sm = cur_bps;
         stats->launches = launches;
         stats->p_launches = p_n;
         stats->u_launches = u_n;

@@ -129,3 +129,26 @@ def test_graph_replay_equals_direct_launches():
     assert np.array_equal(ia, ib) and np.array_equal(ra, rb, equal_nan=True)
     for a, b_ in zip(ua, ub):
         assert np.array_equal(a.view(np.uint32), b_.view(np.uint32))
+
+
+def test_tile_shape_tuner_keeps_the_results():
+    """The tuner times three tile shapes on the first check intervals of the
+    solve itself; the per-voxel arithmetic does not depend on the tile, so
+    with a fixed iteration count u is the same bits tuned and untuned, and a
+    second batch of the same shape reuses the tuned shape."""
+    from miccai2016_gb300.batched import BatchedCut
+    vols = [_volume(8, (64, 64, 64))]
+    insts = [dict(volume=0, weighting=w, decay=d, eigs=ATV) for w in (0.01, 0.05, 0.2, 1.0) for d in (1.0, 30.0)]
+    p = BatchedCut.CutParameters()
+    p.num_iter, p.update, p.error_bound = 150, 30, -1.0
+    res = []
+    for tune in (False, True, True):
+        b = BatchedCut(p)
+        dv = [b.prepare_volume(v["img"], v["quats"], v["cs"], v["ct"], grad2=v["grad2"]) for v in vols]
+        us = b.solve(dv, insts, tune=tune)
+        res.append(([u.cpu().numpy() for u in us], b.last_iterations.copy(), b.last_blocks_per_sm))
+    assert res[0][2] == 16 and res[1][2] in (8, 16, 32) and res[2][2] == res[1][2]
+    for k in range(len(insts)):
+        assert res[0][1][k] == res[1][1][k] == 150
+        assert np.array_equal(res[0][0][k].view(np.uint32), res[1][0][k].view(np.uint32))
+        assert np.array_equal(res[2][0][k].view(np.uint32), res[1][0][k].view(np.uint32))
