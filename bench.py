@@ -411,9 +411,20 @@ def run_batched_grid(plain_sample=17):
     torch.cuda.synchronize()
     batched_s = e0.elapsed_time(e1) / 1000.0
     iters = bc.last_iterations.copy()
+    tuned_bps = bc.last_blocks_per_sm
     truth_d = torch.from_numpy(truth).cuda()
     dice_b = np.asarray(fast_dice(us, truth_d))
     del us
+    # the same batch with the default tile shape and with direct launches
+    variants = {}
+    for name, kw in (("default_tile_shape", dict(tune=False)), ("no_graphs", dict(graphs=False))):
+        e0.record(stream)
+        vu = bc.solve([vol], insts, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        variants[name] = {"s": e0.elapsed_time(e1) / 1000.0, "blocks_per_sm": bc.last_blocks_per_sm,
+                          "same_iterations": bool(np.array_equal(bc.last_iterations, iters))}
+        del vu
     best = int(np.argmax(dice_b))
     # plain path on a sample: the decays of the best weighting (17 instances)
     wi = best // len(cfg["decays"])
@@ -453,6 +464,7 @@ def run_batched_grid(plain_sample=17):
             "best_dice_fast": float(dice_b[best]), "best_weighting": grid[best][0], "best_decay": grid[best][1],
             "max_dice_diff_vs_plain": float(np.max(np.abs(dice_b[sample] - dice_p))),
             "iteration_diff_vs_plain": int(np.max(np.abs(iters[sample] - np.asarray(plain_iters)))),
+            "tuned_blocks_per_sm": tuned_bps, "variants": variants,
             "shared_preparation_s": prep_s, "preparation_stages_s": stages,
             "ridge_points": cut["ridge_points"]}
 

@@ -376,8 +376,11 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     }
     M16_CUDA_TRY(configure(start_bps));
     const bool timed_solve = stats && stats->time_kernels;
-    if (timed_solve || (stats && (stats->flags & M16_BATCH_NO_TUNE)) || (int64_t)work.size() < kTuneMinItems ||
-        params->num_iter < 4 * params->update)
+    // one-lane groups (ragged batches) run the single solve's sweep bodies,
+    // whose tile shape is already tuned; only four-lane groups are tuned
+    bool any4 = false;
+    for (int g = 0; g < ngroups; ++g) any4 = any4 || hg[g].lanes == kLanes;
+    if (timed_solve || !any4 || (int64_t)work.size() < kTuneMinItems || params->num_iter < 4 * params->update)
         tune = false;
 
     const int update = params->update;

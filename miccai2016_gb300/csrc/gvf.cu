@@ -70,7 +70,7 @@ __global__ void gvf_init_kernel(const float *__restrict__ v3, const float *__res
 #define M16_GVF_ZB 2
 #endif
 #ifndef M16_GVF_MINB
-#define M16_GVF_MINB 4   // 4 blocks per SM: 64 registers, measured fastest (profiles/gvf_sweep_256cube.md)
+#define M16_GVF_MINB 4   // 4 blocks per SM caps the sweep at 64 registers: measured fastest on GB300
 #endif
 constexpr int kGvfZB = M16_GVF_ZB;
 
