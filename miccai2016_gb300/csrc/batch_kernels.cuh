@@ -107,6 +107,17 @@ inline int batch_zc(int d0, int d1, int d2, int ngroups_of_volume, int blocks_pe
     return (int)zc;
 }
 
+// One z-chunk for every volume of a launch: the launch covers the tiles of
+// all its groups, so the target number of blocks applies to their sum
+// (total_column_slices = sum over groups of d0 x the volume's 32 x 8 columns).
+inline int batch_zc_total(int64_t total_column_slices, int blocks_per_sm = M16_BATCH_BLOCKS_PER_SM)
+{
+    int64_t zc = total_column_slices / ((int64_t)blocks_per_sm * kSMs);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(32, zc));
+}
+
+inline int64_t column_slices(int d0, int d1, int d2) { return (int64_t)d0 * div_up(d2, kBX) * div_up(d1, kBY); }
+
 __device__ __forceinline__ float lane_of(const float4 &v, int l)
 {
     return l == 0 ? v.x : (l == 1 ? v.y : (l == 2 ? v.z : v.w));

@@ -117,13 +117,16 @@ inline BatchLayout batch_layout(const m16_batch_volume *vols, int nvol, const m1
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
     std::vector<int64_t> tiles(nvol);
+    int64_t total_cs = 0;
+    for (int v = 0; v < nvol; ++v)
+        total_cs += column_slices(vols[v].d0, vols[v].d1, vols[v].d2) * P.ngroups_of_vol[v];
     for (int v = 0; v < nvol; ++v) {
         const int64_t n = (int64_t)vols[v].d0 * vols[v].d1 * vols[v].d2;
         L.q4.push_back(take(n * 16));
         L.maxpart.push_back(take(kMaxBlocks * 4));
         // sized for the candidate with the most (smallest) tiles
         int zc = 32;
-        for (int c : kTuneBps) zc = std::min(zc, batch_zc(vols[v].d0, vols[v].d1, vols[v].d2, P.ngroups_of_vol[v], c));
+        for (int c : kTuneBps) zc = std::min(zc, batch_zc_total(total_cs, c));
         tiles[v] = div_up(vols[v].d2, kBX) * div_up(vols[v].d1, kBY) * div_up(vols[v].d0, zc);
     }
     L.total_blocks = 0;
@@ -206,7 +209,7 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         const m16_batch_volume &V = vols[v];
         VolDev &d = hv[v];
         d.d0 = V.d0; d.d1 = V.d1; d.d2 = V.d2;
-        d.zc = batch_zc(V.d0, V.d1, V.d2, P.ngroups_of_vol[v]);   // set again by configure()
+        d.zc = 1;   // set by configure()
         d.tx = (int)div_up(V.d2, kBX); d.ty = (int)div_up(V.d1, kBY); d.tz = (int)div_up(V.d0, d.zc);
         const double *sc = V.scaling;
         const double smin = fmin(sc[0], fmin(sc[1], sc[2]));
@@ -334,10 +337,12 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     // slots, the work list (the volumes' max / denominator fields written by
     // the set-up kernels are left alone: only zc..tz are copied)
     int cur_bps = 0;
+    int64_t total_cs = 0;
+    for (int v = 0; v < nvol; ++v) total_cs += column_slices(hv[v].d0, hv[v].d1, hv[v].d2) * P.ngroups_of_vol[v];
     auto configure = [&](int bps) -> cudaError_t {
         for (int v = 0; v < nvol; ++v) {
             VolDev &d = hv[v];
-            d.zc = batch_zc(d.d0, d.d1, d.d2, P.ngroups_of_vol[v], bps);
+            d.zc = batch_zc_total(total_cs, bps);
             d.tz = (int)div_up(d.d0, d.zc);
             cudaError_t e = cudaMemcpyAsync((char *)(dvols + v) + offsetof(VolDev, zc), &d.zc, 4 * sizeof(int),
                                             cudaMemcpyHostToDevice, st);
