@@ -391,6 +391,35 @@ int m16_adjust_nonridge_signs_indexed(float *dirs3, int32_t d0, int32_t d1, int3
                                       const float *rdirs, int64_t num_ridge, const double *scaling3,
                                       void *workspace, size_t workspace_bytes, void *stream);
 
+/* ---- ridge minimum spanning tree, local phase --------------------------------- */
+
+/* Workspace bytes of m16_ridge_mst_local (0 for invalid sizes). */
+size_t m16_ridge_mst_workspace_bytes(int64_t num_points, const int32_t *box_dims3, int32_t n_offsets);
+
+/*
+ * The local phase of the ridge-point minimum spanning tree that replaces
+ * minimum_spanning_tree(squareform(pdist(...))) of
+ * AdvancedAdjuster._adjust_ridge_directions (adjust_directions.py:374-379):
+ * the minimum spanning forest, in the total order (weight, i, j) of edges
+ * (i < j), of the candidate edges between points whose offset is one of
+ * `offsets3` (n_offsets x 3, each lexicographically positive, host) and whose
+ * float64 length is <= r.  Lengths are computed as
+ * sqrt((d0 d0 + d1 d1) + d2 d2) with d = p_i * voxel_size - p_j * voxel_size,
+ * every step rounded, as numpy computes them.  Boruvka rounds on the device;
+ * the forest is unique, so the edges are exactly those of Kruskal's algorithm
+ * in that order.
+ *   pts3        num_points x 3 int32 (device), distinct points inside the box
+ *   box_lo3, box_dims3   host: the box holding every point
+ *   voxel_size3 host
+ *   edges       device, 2 x (num_points - 1) int32 (output pairs i < j)
+ *   n_edges     host: number of edges written
+ * Points outside the box or two points on one cell return M16_ERR_BAD_ARG.
+ * Synchronizes `stream`.
+ */
+int m16_ridge_mst_local(const int32_t *pts3, int64_t num_points, const int32_t *box_lo3, const int32_t *box_dims3,
+                        const double *voxel_size3, const int32_t *offsets3, int32_t n_offsets, double r,
+                        int32_t *edges, int64_t *n_edges, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- per-volume cut inputs and scoring --------------------------------------- */
 
 /*

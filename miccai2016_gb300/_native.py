@@ -119,6 +119,11 @@ def _declare(L):
     L.m16_complete_transformations.argtypes = [_vp, _i64, _vp, _vp]
     L.m16_adjust_nonridge_signs.restype = ctypes.c_int
     L.m16_adjust_nonridge_signs.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp, _i64, _vp, _vp]
+    L.m16_ridge_mst_workspace_bytes.restype = _sz
+    L.m16_ridge_mst_workspace_bytes.argtypes = [_i64, _vp, _i32]
+    L.m16_ridge_mst_local.restype = ctypes.c_int
+    L.m16_ridge_mst_local.argtypes = [_vp, _i64, _vp, _vp, _vp, _vp, _i32, _f64, _vp, ctypes.POINTER(_i64), _vp, _sz,
+                                      _vp]
     L.m16_capacities.restype = ctypes.c_int
     L.m16_capacities.argtypes = [_vp, _i32, _i32, _i32, _f64, _f64, _vp, _vp, _vp, _vp]
     L.m16_fast_dice_workspace_bytes.restype = _sz

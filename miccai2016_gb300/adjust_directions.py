@@ -5,9 +5,10 @@ same name (src/processing/adjust_directions.py).
 
 AdvancedAdjuster keeps the reference's sequence (adjust_directions.py:213-256):
 ridge candidates on the GPU, hysteresis on the host, main directions on the
-GPU, the minimum spanning tree over the ridge points and the sign propagation
-along it on the host (ridge_mst.py: SciPy's Kruskal tree with a stable order
-of equal distances, without the reference's dense R x R matrix), ridge
+GPU, the minimum spanning tree over the ridge points (ridge_mst.py: the tree
+of SciPy's Kruskal with a stable order of equal distances, without the
+reference's dense R x R matrix; its local phase in Boruvka rounds on the
+GPU), the sign propagation along it on the host, ridge
 cleaning on the host, and the nearest-ridge sign flip of every voxel on the
 GPU (m16_adjust_nonridge_signs_indexed: the reference's brute-force nearest
 ridge point, found through a cell index of the ridge points).  TransformationCompleter
@@ -28,6 +29,10 @@ from .ridge_mst import propagate_signs, ridge_mst_edges
 
 class AdvancedAdjuster(TreePrintable):
     """adjust_directions.py:25-446"""
+
+    # where the local phase of the ridge MST runs: "gpu" (m16_ridge_mst_local)
+    # or "host" (the same edges with SciPy's Kruskal)
+    mst_local = "gpu"
 
     def __init__(self, threshold, qeigs, response, voxel_size=1, ridge_detection_only=False, clean_ridge=True,
                  loader=None):
@@ -202,7 +207,7 @@ class AdvancedAdjuster(TreePrintable):
         coords = np.argwhere(labeled_ridge)   # C order, as zip(*np.where(...))
         if len(coords) == 0:
             raise ValueError("no ridge points: nothing to propagate directions along")
-        a, b = ridge_mst_edges(coords, self.voxel_size, join_components=join_components)
+        a, b = ridge_mst_edges(coords, self.voxel_size, join_components=join_components, local=self.mst_local)
         dirs = main_dirs[coords[:, 0], coords[:, 1], coords[:, 2]]
         adjusted = propagate_signs(len(coords), a, b, dirs)
         return np.asarray(coords, dtype=np.uint16, order="C"), adjusted

@@ -318,7 +318,9 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     for (int g = 0; g < ngroups; ++g) gactive[g] = hmask[g] != kAllLanes;
     int seg[5] = {0, 0, 0, 0, 0};   // segment k: items seg[k] .. seg[k + 1] - 1
     auto kind_of = [&](int g) { return (hg[g].lanes == kLanes ? 0 : 2) + (hg[g].has_alpha ? 0 : 1); };
+    int work_version = 0;   // bumped whenever the work list (and its segments) is rebuilt
     auto build_work = [&](std::vector<int2> &w) {
+        ++work_version;
         w.clear();
         for (int k = 0; k < 4; ++k) {
             seg[k] = (int)w.size();
@@ -449,6 +451,7 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int graph_launches = 0;
+    int graph_version = -1;   // the work list the graph was captured from
     auto drop_graph = [&]() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
@@ -521,7 +524,11 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         if (it >= params->num_iter) {
             // tuning ran the last iterations
         } else if (use_graph && end - it == chunk && it % update == 0) {
+            // a graph holds the launch sizes and work-list segments it was
+            // captured with: replay it only for the same work list
+            if (gexec && graph_version != work_version) drop_graph();
             if (!gexec) {
+                graph_version = work_version;
                 M16_BT_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
                 graph_launches = 0;
                 for (int k = 0; k < chunk; ++k) graph_launches += enqueue_iteration(cap, (k % update) == 0, false);

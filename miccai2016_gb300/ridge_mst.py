@@ -53,21 +53,10 @@ def _kruskal_by_order(n, i, j, order_keys):
     return t.row.astype(np.int64), t.col.astype(np.int64)
 
 
-def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True):
-    """Edges (a, b) of the (weight, i, j)-ordered Euclidean MST of integer
-    points (R x 3, axis order 0, 1, 2) with per-axis voxel size.  With
-    join_components=False only the local phase runs: the result is the MST
-    minus its edges longer than r, i.e. a spanning tree of every group of
-    points linked by steps not longer than r (each 26-connected set lies in
-    one such group)."""
-    pts = np.asarray(points, dtype=np.int64)
-    R = len(pts)
-    if R < 2:
-        return np.zeros(0, np.int64), np.zeros(0, np.int64)
-    vs = np.asarray(np.multiply(np.ones(3), voxel_size), np.float64)
-    u = np.multiply(pts, vs)   # the coordinates pdist sees
+def _local_offsets(vs):
+    """r = |voxel size| and every integer offset (one of each +- pair, the
+    lexicographically positive one) with scaled length <= r."""
     r = float(np.sqrt(np.sum(vs * vs)))
-    # all integer offsets with scaled length <= r, one of each +-pair
     ext = [int(np.floor(r / vs[k] + 1e-9)) for k in range(3)]
     offsets = []
     for off in itertools.product(*[range(-e, e + 1) for e in ext]):
@@ -75,6 +64,14 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True):
             continue
         if np.sqrt(sum((off[k] * vs[k]) ** 2 for k in range(3))) <= r * (1 + 1e-12):
             offsets.append(off)
+    return r, offsets
+
+
+def _local_mst_host(pts, vs, r, offsets):
+    """The local phase on the host: Kruskal over the candidate edges in
+    (weight, i, j) order."""
+    R = len(pts)
+    u = np.multiply(pts, vs)   # the coordinates pdist sees
     lo = pts.min(0)
     dims = pts.max(0) - lo + 1
     grid = np.full(tuple(int(d) for d in dims), -1, np.int64)
@@ -95,7 +92,55 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True):
     w = _weights(u, i, j)
     keep = w <= r   # exactly the edges not longer than r
     i, j, w = i[keep], j[keep], w[keep]
-    ta, tb = _kruskal_by_order(R, i, j, (j, i, w))
+    return _kruskal_by_order(R, i, j, (j, i, w))
+
+
+def _local_mst_gpu(pts, vs, r, offsets):
+    """The local phase on the GPU (m16_ridge_mst_local, Boruvka rounds in the
+    same (weight, i, j) order): the same edge set as _local_mst_host."""
+    import ctypes
+    from . import _native as N
+    torch = N.torch_mod()
+    L = N.lib()
+    R = len(pts)
+    lo = pts.min(0).astype(np.int32)
+    dims = (pts.max(0) - pts.min(0) + 1).astype(np.int32)
+    offs = np.ascontiguousarray(np.asarray(offsets, np.int32).reshape(-1, 3))
+    d_pts = torch.from_numpy(np.ascontiguousarray(pts, np.int32)).to(N.device())
+    edges = torch.empty((max(R - 1, 1), 2), dtype=torch.int32, device=N.device())
+    ws = N.workspace(L.m16_ridge_mst_workspace_bytes(R, dims.ctypes.data_as(ctypes.c_void_p), len(offs)))
+    vsc = (ctypes.c_double * 3)(*[float(v) for v in vs])
+    ne = ctypes.c_int64(0)
+    st = L.m16_ridge_mst_local(N.ptr(d_pts), R, lo.ctypes.data_as(ctypes.c_void_p),
+                               dims.ctypes.data_as(ctypes.c_void_p), vsc, offs.ctypes.data_as(ctypes.c_void_p),
+                               len(offs), float(r), N.ptr(edges), ctypes.byref(ne), N.ptr(ws), ws.numel(),
+                               N.stream_ptr())
+    N.check("m16_ridge_mst_local", st)
+    e = edges[:ne.value].cpu().numpy().astype(np.int64)
+    return e[:, 0], e[:, 1]
+
+
+def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, local="gpu"):
+    """Edges (a, b) of the (weight, i, j)-ordered Euclidean MST of integer
+    points (R x 3, axis order 0, 1, 2, distinct) with per-axis voxel size.
+    With join_components=False only the local phase runs: the result is the
+    MST minus its edges longer than r, i.e. a spanning tree of every group of
+    points linked by steps not longer than r (each 26-connected set lies in
+    one such group).  local selects where the local phase runs ("gpu", the
+    default, or "host"); both give the same edges."""
+    pts = np.asarray(points, dtype=np.int64)
+    R = len(pts)
+    if R < 2:
+        return np.zeros(0, np.int64), np.zeros(0, np.int64)
+    vs = np.asarray(np.multiply(np.ones(3), voxel_size), np.float64)
+    u = np.multiply(pts, vs)   # the coordinates pdist sees
+    r, offsets = _local_offsets(vs)
+    if local == "gpu":
+        ta, tb = _local_mst_gpu(pts, vs, r, offsets)
+    elif local == "host":
+        ta, tb = _local_mst_host(pts, vs, r, offsets)
+    else:
+        raise ValueError("local must be 'gpu' or 'host'")
     # global phase: join the local trees
     forest = scipy.sparse.coo_matrix((np.ones(len(ta)), (ta, tb)), shape=(R, R))
     ncomp, comp = connected_components(forest, directed=False)

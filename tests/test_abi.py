@@ -153,3 +153,24 @@ def test_capacities_and_dice_validate_before_touching_the_gpu(lib):
     ptrs = (ctypes.c_void_p * 3)(256, 512, 768)
     assert lib.m16_fast_dice(ptrs, 3, 100, fake, out, fake, nb - 1, None) == N.M16_ERR_WORKSPACE
     assert lib.m16_fast_dice(ptrs, 0, 100, fake, out, fake, nb, None) == N.M16_ERR_BAD_ARG
+
+
+def test_ridge_mst_validates_before_touching_the_gpu(lib):
+    from miccai2016_gb300 import _native as N
+    fake = ctypes.c_void_p(256)
+    dims = (ctypes.c_int32 * 3)(4, 4, 4)
+    lo = (ctypes.c_int32 * 3)(0, 0, 0)
+    vs = (ctypes.c_double * 3)(1, 1, 1)
+    offs = (ctypes.c_int32 * 3)(0, 0, 1)
+    nb = lib.m16_ridge_mst_workspace_bytes(10, dims, 1)
+    assert nb >= 64 * 4 + 10 * 24
+    assert lib.m16_ridge_mst_workspace_bytes(0, dims, 1) == 0
+    n = ctypes.c_int64(-1)
+    call = lambda R, d, v, r, wsb: lib.m16_ridge_mst_local(fake, R, lo, d, v, offs, 1, r, fake, ctypes.byref(n),
+                                                           fake, wsb, None)
+    assert call(0, dims, vs, 1.7, nb) == N.M16_ERR_BAD_SHAPE
+    assert call(10, (ctypes.c_int32 * 3)(4, 0, 4), vs, 1.7, nb) == N.M16_ERR_BAD_SHAPE
+    assert call(10, dims, (ctypes.c_double * 3)(1, -1, 1), 1.7, nb) == N.M16_ERR_BAD_ARG
+    assert call(10, dims, vs, 0.0, nb) == N.M16_ERR_BAD_ARG
+    assert call(10, dims, vs, 1.7, nb - 1) == N.M16_ERR_WORKSPACE
+    assert call(1, dims, vs, 1.7, lib.m16_ridge_mst_workspace_bytes(1, dims, 1)) == N.M16_OK and n.value == 0

@@ -152,3 +152,27 @@ def test_tile_shape_tuner_keeps_the_results():
         assert res[0][1][k] == res[1][1][k] == 150
         assert np.array_equal(res[0][0][k].view(np.uint32), res[1][0][k].view(np.uint32))
         assert np.array_equal(res[2][0][k].view(np.uint32), res[1][0][k].view(np.uint32))
+
+
+def test_tuning_graphs_and_a_shrinking_work_list_together():
+    """Four-lane groups and a one-lane group in one batch, tuned, replayed as
+    graphs, with instances stopping at different checks so the work list
+    shrinks while the shape is tuned: every instance still gives its plain
+    solve (a graph is never replayed over a work list it was not captured
+    from)."""
+    from miccai2016_gb300.batched import BatchedCut
+    vols = [_volume(9, (48, 48, 48))]
+    insts = [dict(volume=0, weighting=w, decay=d, eigs=ATV) for w in (0.003, 0.03, 0.3, 3.0)
+             for d in (0.3, 3.0, 30.0)] + [dict(volume=0, weighting=0.05, decay=1.0, eigs=TV)]
+    p = BatchedCut.CutParameters()
+    p.num_iter, p.update, p.error_bound = 1200, 10, 2e-3
+    b = BatchedCut(p)
+    dv = [b.prepare_volume(v["img"], v["quats"], v["cs"], v["ct"], grad2=v["grad2"]) for v in vols]
+    us = [u.cpu().numpy() for u in b.solve(dv, insts, graphs=True, tune=True)]
+    its = b.last_iterations
+    assert len(set(its.tolist())) > 2
+    for k, inst in enumerate(insts):
+        u, it = _plain(vols[0], inst, 1200, 10, 2e-3)
+        assert abs(int(its[k]) - it) <= 10
+        if int(its[k]) == it:
+            assert np.max(np.abs(us[k] - u)) <= U_TOL

@@ -91,7 +91,7 @@ def test_sparse_mst_equals_the_dense_stable_kruskal(vs):
     for _ in range(4):
         pts = np.unique(np.concatenate([rng.randint(0, 10, (120, 3)) + rng.randint(0, 35, 3) for _ in range(4)]), axis=0)
         pts = pts[rng.permutation(len(pts))]
-        a, b = ridge_mst_edges(pts, vs)
+        a, b = ridge_mst_edges(pts, vs, local="host")
         t = A.stable_mst(pts, vs).tocoo()
         assert set(zip(np.minimum(a, b), np.maximum(a, b))) == set(zip(np.minimum(t.row, t.col),
                                                                        np.maximum(t.row, t.col)))
@@ -110,6 +110,7 @@ def test_ridge_directions_and_cleaning_match_the_reference_logic():
             p = p + rng.randint(-1, 2, 3)
     main = rng.normal(size=shape + (3,)).astype(np.float32)
     obj = AdvancedAdjuster((0.01, 0.3), np.zeros(shape + (3,), np.float32), np.zeros(shape, np.float32))
+    obj.mst_local = "host"
     c1, d1 = A.adjust_ridge_directions(ridge, main, (1.0, 1.0, 1.0))
     c2, d2 = obj._adjust_ridge_directions(ridge, main)
     assert np.array_equal(c1, c2) and np.array_equal(_bits(d1), _bits(d2))
@@ -131,6 +132,7 @@ def test_cleaning_is_the_same_without_joining_the_segments():
             p = p + rng.randint(-1, 2, 3)
     main = rng.normal(size=shape + (3,)).astype(np.float32)
     obj = AdvancedAdjuster((0.01, 0.3), np.zeros(shape + (3,), np.float32), np.zeros(shape, np.float32))
+    obj.mst_local = "host"
     c1, d1 = obj._adjust_ridge_directions(ridge, main, join_components=True)
     c2, d2 = obj._adjust_ridge_directions(ridge, main, join_components=False)
     with contextlib.redirect_stdout(io.StringIO()):
