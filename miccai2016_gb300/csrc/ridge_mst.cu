@@ -45,7 +45,7 @@ struct MstArgs {
     int *parent;           // R: for roots, the component hooked to
     unsigned long long *minw, *minij;   // R: per root
     int *edges;            // 2 x (R - 1)
-    unsigned long long *ctrl;   // [0] edges so far, [1] walks that hit the limit, [2] bad points
+    unsigned long long *ctrl;   // [0] edges so far, [1] walks at the limit or edge overflow, [2] bad points
 };
 
 constexpr unsigned long long kNone = ~0ull;
@@ -120,6 +120,10 @@ __global__ void mst_hook_kernel(MstArgs a)
         if (a.minij[other] == key && (int)c < other) continue;
         a.parent[c] = other;
         const unsigned long long e = atomicAdd(a.ctrl, 1ull);
+        if (e >= (unsigned long long)(a.R - 1)) {   // a forest has at most R - 1 edges: never expected
+            atomicAdd(a.ctrl + 1, 1ull);
+            continue;
+        }
         a.edges[2 * e] = lo;
         a.edges[2 * e + 1] = hi;
     }
@@ -243,7 +247,7 @@ extern "C" int m16_ridge_mst_local(const int32_t *pts3, int64_t num_points, cons
         M16_CUDA_TRY(cudaGetLastError());
         M16_CUDA_TRY(cudaMemcpyAsync(h, a.ctrl, 16, cudaMemcpyDeviceToHost, st));
         M16_CUDA_TRY(cudaStreamSynchronize(st));
-        if (h[1] != 0) return M16_ERR_TIMEOUT;   // a component walk did not end: never expected
+        if (h[1] != 0) return M16_ERR_TIMEOUT;   // a walk did not end or the edges overflowed: never expected
         if (h[0] == before) break;
         before = h[0];
     }
