@@ -370,7 +370,8 @@ def run_ours(args, cfg):
         line["batched"] = run_batched_grid()
         if args.served_requests > 0:
             from miccai2016_gb300.serving import served_vs_plain
-            line["served"] = served_vs_plain(n_requests=args.served_requests, rate=50.0, pool=8)
+            line["served"] = served_vs_plain(n_requests=args.served_requests, rate=50.0, pool=8,
+                                             max_resident=args.served_max_resident or None)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -719,6 +720,8 @@ def main():
                     help="ragged workload: every k-th of the 15 noise levels")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched grid search and the serving comparison of the default workload")
+    ap.add_argument("--served-max-resident", type=int, default=0,
+                    help="serving comparison: at most this many requests resident at once (0: no limit)")
     ap.add_argument("--served-requests", type=int, default=96,
                     help="requests of the serving comparison (0 skips it)")
     args = ap.parse_args()
