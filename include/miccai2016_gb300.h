@@ -420,6 +420,23 @@ int m16_ridge_mst_local(const int32_t *pts3, int64_t num_points, const int32_t *
                         const double *voxel_size3, const int32_t *offsets3, int32_t n_offsets, double r,
                         int32_t *edges, int64_t *n_edges, void *workspace, size_t workspace_bytes, void *stream);
 
+/* ---- 26-connected labelling ------------------------------------------------------ */
+
+/* Workspace bytes of m16_label26 (0 for invalid sizes). */
+size_t m16_label26_workspace_bytes(int32_t d0, int32_t d1, int32_t d2);
+
+/*
+ * Connected components of a binary volume (mask: uint8, nonzero = foreground)
+ * under 26-connectivity, numbered 1, 2, ... in the raster order of each
+ * component's first voxel and 0 on the background -- exactly the labels and
+ * count of scipy.ndimage.label(mask, structure=np.ones((3, 3, 3))), which the
+ * sign adjustment runs for its hysteresis (ridge_detection.py:80-131) and its
+ * ridge cleaning (adjust_directions.py:290-339).  d0 * d1 * d2 < 2^31.
+ * labels: int32 (device); n_labels: host.  Synchronizes `stream`.
+ */
+int m16_label26(const uint8_t *mask, int32_t d0, int32_t d1, int32_t d2, int32_t *labels, int32_t *n_labels,
+                void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- per-volume cut inputs and scoring --------------------------------------- */
 
 /*

@@ -119,6 +119,10 @@ def _declare(L):
     L.m16_complete_transformations.argtypes = [_vp, _i64, _vp, _vp]
     L.m16_adjust_nonridge_signs.restype = ctypes.c_int
     L.m16_adjust_nonridge_signs.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp, _i64, _vp, _vp]
+    L.m16_label26_workspace_bytes.restype = _sz
+    L.m16_label26_workspace_bytes.argtypes = [_i32, _i32, _i32]
+    L.m16_label26.restype = ctypes.c_int
+    L.m16_label26.argtypes = [_vp, _i32, _i32, _i32, _vp, ctypes.POINTER(_i32), _vp, _sz, _vp]
     L.m16_ridge_mst_workspace_bytes.restype = _sz
     L.m16_ridge_mst_workspace_bytes.argtypes = [_i64, _vp, _i32]
     L.m16_ridge_mst_local.restype = ctypes.c_int

@@ -19,9 +19,9 @@ from __future__ import annotations
 import ctypes
 
 import numpy as np
-from scipy.ndimage import label
 
 from . import _native as N
+from .labeling import label26
 from .parameters import TreePrintable
 from .ridge_detection import RawRidgeDetector, hysteresis_threshold
 from .ridge_mst import propagate_signs, ridge_mst_edges
@@ -33,6 +33,9 @@ class AdvancedAdjuster(TreePrintable):
     # where the local phase of the ridge MST runs: "gpu" (m16_ridge_mst_local)
     # or "host" (the same edges with SciPy's Kruskal)
     mst_local = "gpu"
+    # where the 26-connected labelling of the hysteresis and the cleaning
+    # runs: "gpu" (m16_label26) or "host" (scipy.ndimage.label, the same labels)
+    labeler = "gpu"
 
     def __init__(self, threshold, qeigs, response, voxel_size=1, ridge_detection_only=False, clean_ridge=True,
                  loader=None):
@@ -158,7 +161,7 @@ class AdvancedAdjuster(TreePrintable):
         ridge = np.require(ridge, np.float32, ["C", "A", "W"])
         if self._hysteresis:
             sure = np.logical_and(ridge, self.response >= self.threshold[1])
-            ridge[:] = hysteresis_threshold(ridge, sure)
+            ridge[:] = hysteresis_threshold(ridge, sure, labeler=self.labeler)
         self.__ridge = ridge
         return ridge
 
@@ -167,7 +170,7 @@ class AdvancedAdjuster(TreePrintable):
         directions are longest (adjust_directions.py:290-339).  Per segment the
         directions are summed in the reference's order (C order of the voxels)."""
         scaled = ridge_dirs * self.__voxel_size   # float32 * tuple -> float64, as in the reference
-        components = label(labeled_ridge, structure=np.ones((3, 3, 3), dtype=int))[0]
+        components = label26(labeled_ridge, where=self.labeler)[0]
         labels = np.unique(components)[1:]
         point_label = components[tuple(np.asarray(ridge_coords, np.intp).T)]
         order = np.argsort(point_label, kind="stable")

@@ -1,0 +1,216 @@
+// label26.cu -- connected components of a binary volume under 26-connectivity
+// on the GPU, numbered exactly as scipy.ndimage.label numbers them with a
+// 3 x 3 x 3 structure of ones.  The sign adjustment labels its ridge this way
+// twice: the hysteresis (src/processing/ridge_detection.py:80-131: the union
+// of the 26-connected candidate components holding a sure voxel) and the
+// ridge cleaning (src/processing/adjust_directions.py:290-339).
+//
+// Union-find over voxel indices: every foreground voxel starts as its own
+// root; for each of its 13 forward neighbours a lock-free union hooks the
+// larger of the two roots onto the smaller, so every component
+// ends with the smallest linear index of its voxels as root (a root is
+// hooked only while it is still a root, by compare-and-swap).  SciPy numbers
+// components 1, 2, ... in the raster order of their first voxel, which is the
+// order of those smallest indices: a component's label is one plus the number
+// of roots before its root, an exclusive scan of the root flags.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace m16 {
+namespace {
+
+constexpr int kFindLimit = 1 << 26;   // pointer walks never get this long: a bound, not a wait
+
+__device__ __forceinline__ int find_root(const int *parent, int i, unsigned long long *err)
+{
+    int steps = 0;
+    int p = parent[i];
+    while (p != i) {
+        i = p;
+        p = parent[i];
+        if (++steps > kFindLimit) { atomicAdd(err, 1ull); break; }
+    }
+    return i;
+}
+
+__global__ void lb_init_kernel(const uint8_t *__restrict__ mask, int64_t n, int *__restrict__ parent)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        parent[i] = mask[i] ? (int)i : -1;
+}
+
+// union of each foreground voxel with its forward 26-neighbours
+__global__ void lb_union_kernel(const uint8_t *__restrict__ mask, int d0, int d1, int d2, int *parent,
+                                unsigned long long *err)
+{
+    const int64_t s0 = (int64_t)d1 * d2, n = s0 * d0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!mask[i]) continue;
+        const int z = (int)(i / s0), y = (int)((i / d2) % d1), x = (int)(i % d2);
+        // forward half of the 26-neighbourhood: (dz, dy, dx) > (0, 0, 0)
+        for (int k = 14; k < 27; ++k) {
+            const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
+            const int zz = z + dz, yy = y + dy, xx = x + dx;
+            if (zz >= d0 || yy < 0 || yy >= d1 || xx < 0 || xx >= d2) continue;
+            const int64_t j = i + (int64_t)dz * s0 + (int64_t)dy * d2 + dx;
+            if (!mask[j]) continue;
+            int a = find_root(parent, (int)i, err), b = find_root(parent, (int)j, err);
+            int tries = 0;
+            while (a != b && tries++ < kFindLimit) {
+                if (a < b) { const int t = a; a = b; b = t; }   // hook the larger root a onto b
+                // only while a is still a root: re-pointing a hooked node
+                // would cut its subtree off its set
+                const int old = atomicCAS(parent + a, a, b);
+                if (old == a) break;
+                a = find_root(parent, old, err);               // a was hooked meanwhile: retry from the roots
+                b = find_root(parent, b, err);
+            }
+            if (tries >= kFindLimit) atomicAdd(err, 1ull);
+        }
+    }
+}
+
+// every voxel points at its root; roots are flagged for the numbering
+__global__ void lb_compress_kernel(int64_t n, int *parent, unsigned *__restrict__ is_root, unsigned long long *err)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int p = parent[i];
+        if (p < 0) { is_root[i] = 0u; continue; }
+        const int r = find_root(parent, (int)i, err);
+        parent[i] = r;
+        is_root[i] = r == (int)i ? 1u : 0u;
+    }
+}
+
+// exclusive scan of the root flags in blocks of 1024, then of the block sums
+constexpr int kScan = 1024;
+
+__global__ void __launch_bounds__(256) lb_scan_local_kernel(const unsigned *__restrict__ flag, int64_t n,
+                                                            unsigned *__restrict__ rank, unsigned *__restrict__ bsum)
+{
+    __shared__ unsigned s[256];
+    const int64_t base = blockIdx.x * (int64_t)kScan + 4 * threadIdx.x;
+    unsigned v[4], t = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        v[k] = base + k < n ? flag[base + k] : 0u;
+        t += v[k];
+    }
+    s[threadIdx.x] = t;
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {
+        const unsigned add = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0u;
+        __syncthreads();
+        s[threadIdx.x] += add;
+        __syncthreads();
+    }
+    unsigned run = s[threadIdx.x] - t;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < n) rank[base + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 255) bsum[blockIdx.x] = s[255];
+}
+
+// sequential exclusive scan of the block sums by one block, 1024 per pass
+__global__ void __launch_bounds__(1024) lb_scan_blocks_kernel(unsigned *bsum, int64_t nblocks, unsigned *total)
+{
+    __shared__ unsigned s[1024];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0u;
+    __syncthreads();
+    for (int64_t base = 0; base < nblocks; base += 1024) {
+        const int64_t i = base + threadIdx.x;
+        const unsigned v = i < nblocks ? bsum[i] : 0u;
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {
+            const unsigned add = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0u;
+            __syncthreads();
+            s[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (i < nblocks) bsum[i] = carry + s[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += s[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// labels = 1 + rank of the voxel's root (0 on the background)
+__global__ void lb_number_kernel(const int *__restrict__ parent, const unsigned *__restrict__ rank,
+                                 const unsigned *__restrict__ bsum, int64_t n, int32_t *__restrict__ labels)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = parent[i];
+        labels[i] = r < 0 ? 0 : (int32_t)(rank[r] + bsum[r / kScan] + 1u);
+    }
+}
+
+struct LbLayout {
+    size_t parent, flag, rank, bsum, ctrl, total;
+    int64_t nblocks;
+};
+
+inline LbLayout lb_layout(int64_t n)
+{
+    LbLayout L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
+    L.nblocks = div_up(n, kScan);
+    L.parent = take((size_t)n * 4);
+    L.flag = take((size_t)n * 4);
+    L.rank = take((size_t)n * 4);
+    L.bsum = take((size_t)(L.nblocks + 1) * 4);
+    L.ctrl = take(16);
+    L.total = off;
+    return L;
+}
+
+inline int lb_blocks(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(16 * kSMs, div_up(n, 256))); }
+
+}  // namespace
+}  // namespace m16
+
+using namespace m16;
+
+extern "C" size_t m16_label26_workspace_bytes(int32_t d0, int32_t d1, int32_t d2)
+{
+    if (d0 < 1 || d1 < 1 || d2 < 1 || (int64_t)d0 * d1 * d2 > (int64_t)INT32_MAX) return 0;
+    return lb_layout((int64_t)d0 * d1 * d2).total;
+}
+
+extern "C" int m16_label26(const uint8_t *mask, int32_t d0, int32_t d1, int32_t d2, int32_t *labels,
+                           int32_t *n_labels, void *workspace, size_t workspace_bytes, void *stream)
+{
+    if (d0 < 1 || d1 < 1 || d2 < 1 || (int64_t)d0 * d1 * d2 > (int64_t)INT32_MAX) return M16_ERR_BAD_SHAPE;
+    if (!mask || !labels || !n_labels) return M16_ERR_BAD_ARG;
+    const int64_t n = (int64_t)d0 * d1 * d2;
+    const LbLayout L = lb_layout(n);
+    if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *ws = (char *)workspace;
+    int *parent = (int *)(ws + L.parent);
+    unsigned *flag = (unsigned *)(ws + L.flag), *rank = (unsigned *)(ws + L.rank), *bsum = (unsigned *)(ws + L.bsum);
+    unsigned long long *ctrl = (unsigned long long *)(ws + L.ctrl);   // [0] walk-limit errors; total at +8
+    M16_CUDA_TRY(cudaMemsetAsync(ctrl, 0, 16, st));
+    lb_init_kernel<<<lb_blocks(n), 256, 0, st>>>(mask, n, parent);
+    lb_union_kernel<<<lb_blocks(n), 256, 0, st>>>(mask, d0, d1, d2, parent, ctrl);
+    lb_compress_kernel<<<lb_blocks(n), 256, 0, st>>>(n, parent, flag, ctrl);
+    lb_scan_local_kernel<<<(unsigned)L.nblocks, 256, 0, st>>>(flag, n, rank, bsum);
+    lb_scan_blocks_kernel<<<1, 1024, 0, st>>>(bsum, L.nblocks, (unsigned *)(ctrl + 1));
+    lb_number_kernel<<<lb_blocks(n), 256, 0, st>>>(parent, rank, bsum, n, labels);
+    M16_CUDA_TRY(cudaGetLastError());
+    unsigned long long h[2] = {0, 0};
+    M16_CUDA_TRY(cudaMemcpyAsync(h, ctrl, 16, cudaMemcpyDeviceToHost, st));
+    M16_CUDA_TRY(cudaStreamSynchronize(st));
+    if (h[0] != 0) return M16_ERR_TIMEOUT;   // a root walk hit its bound: never expected
+    *n_labels = (int32_t)(h[1] & 0xffffffffu);
+    return M16_OK;
+}

@@ -3,13 +3,12 @@ Ridge detection in a vesselness response -- the drop-in for the reference
 module of the same name (src/processing/ridge_detection.py).
 
 RawRidgeDetector runs the in-plane local-maximum test on the GPU
-(m16_detect_ridges, csrc/directions.cu); hysteresis_threshold is host code,
-as in the reference.
+(m16_detect_ridges, csrc/directions.cu); hysteresis_threshold labels the
+candidates' 26-connected components once (on the GPU by default).
 """
 from __future__ import annotations
 
 import numpy as np
-import scipy.ndimage
 
 from . import _native as N
 
@@ -52,7 +51,7 @@ class RawRidgeDetector(object):
         return out if on_device else out.cpu().numpy()
 
 
-def hysteresis_threshold(cand, sure):
+def hysteresis_threshold(cand, sure, labeler="gpu"):
     """ridge_detection.py:80-131: the voxels of `cand` 26-connected (through
     candidates) to a voxel of `sure`, plus `sure` itself.  As in the reference,
     `sure` is overwritten with the result and returned (and `cand` is cleared
@@ -61,10 +60,12 @@ def hysteresis_threshold(cand, sure):
     The reference floods from every sure voxel with an explicit stack; the
     union of its floods is exactly the union of the 26-connected components of
     (cand | sure) that contain a sure voxel, which is computed here with one
-    labelling pass."""
+    labelling pass (labeler: "gpu", m16_label26, or "host", scipy; the same
+    labels)."""
+    from .labeling import label26
     assert cand.shape == sure.shape
     both = np.logical_or(cand, sure)
-    labels, n = scipy.ndimage.label(both, structure=np.ones((3, 3, 3), dtype=int))
+    labels, n = label26(both, where=labeler)
     keep = np.zeros(n + 1, bool)
     keep[np.unique(labels[np.asarray(sure, bool)])] = True
     keep[0] = False

@@ -174,3 +174,15 @@ def test_ridge_mst_validates_before_touching_the_gpu(lib):
     assert call(10, dims, vs, 0.0, nb) == N.M16_ERR_BAD_ARG
     assert call(10, dims, vs, 1.7, nb - 1) == N.M16_ERR_WORKSPACE
     assert call(1, dims, vs, 1.7, lib.m16_ridge_mst_workspace_bytes(1, dims, 1)) == N.M16_OK and n.value == 0
+
+
+def test_label26_validates_before_touching_the_gpu(lib):
+    from miccai2016_gb300 import _native as N
+    fake = ctypes.c_void_p(256)
+    n = ctypes.c_int32(0)
+    nb = lib.m16_label26_workspace_bytes(8, 8, 8)
+    assert nb >= 512 * 12 and lib.m16_label26_workspace_bytes(0, 8, 8) == 0
+    assert lib.m16_label26_workspace_bytes(2048, 2048, 1024) == 0      # beyond 2^31 voxels
+    assert lib.m16_label26(fake, 0, 8, 8, fake, ctypes.byref(n), fake, nb, None) == N.M16_ERR_BAD_SHAPE
+    assert lib.m16_label26(None, 8, 8, 8, fake, ctypes.byref(n), fake, nb, None) == N.M16_ERR_BAD_ARG
+    assert lib.m16_label26(fake, 8, 8, 8, fake, ctypes.byref(n), fake, nb - 1, None) == N.M16_ERR_WORKSPACE

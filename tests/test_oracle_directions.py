@@ -67,7 +67,7 @@ def test_label_hysteresis_equals_the_reference_flood_fill():
         if t % 5 == 0:
             sure |= rng.uniform(size=shape) < 0.02   # sure voxels outside the candidates
         a = A.hysteresis_threshold(cand.copy(), sure.copy())
-        b = hysteresis_threshold(cand.copy(), sure.copy())
+        b = hysteresis_threshold(cand.copy(), sure.copy(), labeler="host")
         assert np.array_equal(a, b)
 
 
@@ -111,6 +111,7 @@ def test_ridge_directions_and_cleaning_match_the_reference_logic():
     main = rng.normal(size=shape + (3,)).astype(np.float32)
     obj = AdvancedAdjuster((0.01, 0.3), np.zeros(shape + (3,), np.float32), np.zeros(shape, np.float32))
     obj.mst_local = "host"
+    obj.labeler = "host"
     c1, d1 = A.adjust_ridge_directions(ridge, main, (1.0, 1.0, 1.0))
     c2, d2 = obj._adjust_ridge_directions(ridge, main)
     assert np.array_equal(c1, c2) and np.array_equal(_bits(d1), _bits(d2))
@@ -133,6 +134,7 @@ def test_cleaning_is_the_same_without_joining_the_segments():
     main = rng.normal(size=shape + (3,)).astype(np.float32)
     obj = AdvancedAdjuster((0.01, 0.3), np.zeros(shape + (3,), np.float32), np.zeros(shape, np.float32))
     obj.mst_local = "host"
+    obj.labeler = "host"
     c1, d1 = obj._adjust_ridge_directions(ridge, main, join_components=True)
     c2, d2 = obj._adjust_ridge_directions(ridge, main, join_components=False)
     with contextlib.redirect_stdout(io.StringIO()):
