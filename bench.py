@@ -152,11 +152,21 @@ def _traffic_summary():
         return None
 
 
-def _cpu_threads():
+def _affinity():
     try:
         return len(os.sched_getaffinity(0))
     except AttributeError:  # pragma: no cover
         return os.cpu_count() or 1
+
+
+# host threads available to the process, read before any OpenMP runtime binds
+# the main thread to one core (OMP_PROC_BIND=close does after its first
+# parallel region)
+_HOST_THREADS = _affinity()
+
+
+def _cpu_threads():
+    return _HOST_THREADS
 
 
 def cpu_baseline(cfg, inp, iters=3):

@@ -129,7 +129,7 @@ __global__ void mf_init_kernel(MfArgs a, const float *__restrict__ img, const fl
 #ifndef M16_MF_FUSED_MINB
 #define M16_MF_FUSED_MINB 3
 #endif
-constexpr int kZB = kMfZB;
+constexpr int kZB = kMfZB > kMfUZB ? kMfZB : kMfUZB;   // z-chunks are whole load batches of both sweeps
 
 __device__ __forceinline__ FlowView flow_view(const MfArgs &a)
 {
