@@ -420,6 +420,31 @@ int m16_ridge_mst_local(const int32_t *pts3, int64_t num_points, const int32_t *
                         const double *voxel_size3, const int32_t *offsets3, int32_t n_offsets, double r,
                         int32_t *edges, int64_t *n_edges, void *workspace, size_t workspace_bytes, void *stream);
 
+/*
+ * Host function (no device work): the signs of the ridge directions along the
+ * tree of AdvancedAdjuster._adjust_ridge_directions (adjust_directions.py:382-415).
+ * order (host, n_order entries): the points in visiting order, each parent
+ * before its children; pred (host, n): each point's parent in that visit;
+ * e (host, n): per point the sign of np.dot(its direction, its parent's
+ * unadjusted direction): 1, -1, 0 (zero: keeps its direction, as does a
+ * restart point such as the root) or 2 (NaN: negated).  s (host, n int8):
+ * output, the final sign of every visited point: 1 where e is 0, -1 where e
+ * is 2, else the parent's sign times e.
+ */
+int m16_compose_signs(int64_t n, const int32_t *order, int64_t n_order, const int32_t *pred, const int8_t *e,
+                      int8_t *s);
+
+/*
+ * Host function (no device work): the visiting order of that propagation over
+ * an undirected forest of n points (n_edges edges ea[k] -- eb[k], host):
+ * breadth first from `root`, then every other tree from its lowest-index
+ * point, as the reference hangs the rest of a forest off the root.  order
+ * (host, n): every point once, parents before children; pred (host, n): each
+ * point's parent, -1 for the root and the other trees' first points.
+ */
+int m16_tree_order(int64_t n, const int32_t *ea, const int32_t *eb, int64_t n_edges, int32_t root, int32_t *order,
+                   int32_t *pred);
+
 /* ---- 26-connected labelling ------------------------------------------------------ */
 
 /* Workspace bytes of m16_label26 (0 for invalid sizes). */

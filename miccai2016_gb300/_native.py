@@ -119,6 +119,10 @@ def _declare(L):
     L.m16_complete_transformations.argtypes = [_vp, _i64, _vp, _vp]
     L.m16_adjust_nonridge_signs.restype = ctypes.c_int
     L.m16_adjust_nonridge_signs.argtypes = [_vp, _i32, _i32, _i32, _vp, _vp, _i64, _vp, _vp]
+    L.m16_tree_order.restype = ctypes.c_int
+    L.m16_tree_order.argtypes = [_i64, _vp, _vp, _i64, _i32, _vp, _vp]
+    L.m16_compose_signs.restype = ctypes.c_int
+    L.m16_compose_signs.argtypes = [_i64, _vp, _i64, _vp, _vp, _vp]
     L.m16_label26_workspace_bytes.restype = _sz
     L.m16_label26_workspace_bytes.argtypes = [_i32, _i32, _i32]
     L.m16_label26.restype = ctypes.c_int

@@ -26,12 +26,15 @@ the squared differences of the scaled coordinates, in float64.
 """
 from __future__ import annotations
 
+import ctypes
 import itertools
 
 import numpy as np
 import scipy.sparse
-from scipy.sparse.csgraph import breadth_first_order, connected_components, minimum_spanning_tree
+from scipy.sparse.csgraph import connected_components, minimum_spanning_tree
 from scipy.spatial import cKDTree
+
+from . import _native as N
 
 
 def _weights(u, i, j):
@@ -98,8 +101,6 @@ def _local_mst_host(pts, vs, r, offsets):
 def _local_mst_gpu(pts, vs, r, offsets):
     """The local phase on the GPU (m16_ridge_mst_local, Boruvka rounds in the
     same (weight, i, j) order): the same edge set as _local_mst_host."""
-    import ctypes
-    from . import _native as N
     torch = N.torch_mod()
     L = N.lib()
     R = len(pts)
@@ -210,49 +211,30 @@ def propagate_signs(n, edges_a, edges_b, dirs, root=0):
     point were the root.
 
     The reference visits the points one by one.  Here all decisions are
-    evaluated at once: with s the sign a point's direction ends up with,
+    evaluated at once: the visiting order and parents come from one traversal
+    (m16_tree_order), and with s the sign a point's direction ends up with,
     np.dot(d_c, s_p d_p) = s_p np.dot(d_c, d_p) bit for bit (negating one
     operand negates every rounded step), so s_c = +1 where np.dot(d_c, d_p)
     is zero (either sign of zero passes ">= 0"), s_c = -1 where it is NaN,
-    and s_c = s_p sign(np.dot(d_c, d_p)) elsewhere; the products along each
-    path to the root (or to such a restart point) are formed by pointer
-    jumping."""
+    and s_c = s_p sign(np.dot(d_c, d_p)) elsewhere; the signs are then
+    composed in one pass in visiting order (m16_compose_signs, host code of
+    the library)."""
     dirs = np.asarray(dirs, dtype=np.float32)
     adjusted = np.ones((n, 3), dtype=np.float32) * np.float32(np.nan)
-    g = scipy.sparse.coo_matrix((np.ones(len(edges_a)), (edges_a, edges_b)), shape=(n, n)).tocsr()
-    ncomp, comp = connected_components(g, directed=False)
-    # the other trees hang off `root` through virtual edges to their
-    # lowest-index points, which restart the propagation
-    _, first = np.unique(comp, return_index=True)
-    starts = np.asarray([f for f in first if comp[f] != comp[root]], np.int64)
-    if len(starts):
-        va = np.concatenate([edges_a, np.full(len(starts), root, np.int64)])
-        vb = np.concatenate([edges_b, starts])
-        g = scipy.sparse.coo_matrix((np.ones(len(va)), (va, vb)), shape=(n, n)).tocsr()
-    order, pred = breadth_first_order(g, root, directed=False, return_predecessors=True)
-    parent = np.arange(n, dtype=np.int64)
-    val = np.ones(n, dtype=np.int8)
-    kids = order[1:]
-    kids = kids[~np.isin(kids, starts)]       # restarts keep their own direction
-    par = pred[kids].astype(np.int64)
-    e = _dot_signs(dirs[kids], dirs[par])
-    chained = (e == 1) | (e == -1)            # a zero dot restarts at +1, a NaN one at -1
-    parent[kids[chained]] = par[chained]
-    val[kids[chained]] = e[chained]
-    own = np.ones(n, dtype=np.int8)           # the absolute sign of a restart point
-    own[kids[e == 2]] = -1
-    # pointer jumping: val[c] becomes the product of the signs from c up to
-    # the first restart r (the root, a start, a zero-dot or NaN point; val of
-    # a restart stays 1, its own sign is applied once at the end)
-    while True:
-        pp = parent[parent]
-        if np.array_equal(pp, parent):
-            break
-        val = val * val[parent]
-        parent = pp
-    val = val * own[parent]
-    reached = np.zeros(n, bool)
-    reached[order] = True
-    neg = val[reached, None] < 0
-    adjusted[reached] = np.where(neg, -dirs[reached], dirs[reached])   # negation flips the sign bit, NaN too
+    L = N.lib()
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    ea = np.ascontiguousarray(edges_a, dtype=np.int32)
+    eb = np.ascontiguousarray(edges_b, dtype=np.int32)
+    order = np.empty(n, np.int32)
+    pred = np.empty(n, np.int32)
+    N.check("m16_tree_order", L.m16_tree_order(n, vp(ea), vp(eb), len(ea), int(root), vp(order), vp(pred)))
+    e = np.zeros(n, dtype=np.int8)            # 0: keeps its direction (the root and each tree's first point)
+    kids = np.nonzero(pred >= 0)[0]
+    e[kids] = _dot_signs(dirs[kids], dirs[pred[kids].astype(np.int64)])
+    # one pass in visiting order: s_c = s_parent * e_c (+1 at zero dots, -1 at NaN dots)
+    sgn = np.ones(n, dtype=np.int8)
+    N.check("m16_compose_signs", L.m16_compose_signs(n, vp(order), n, vp(pred), vp(e), vp(sgn)))
+    val = sgn
+    neg = val[:, None] < 0
+    adjusted[:] = np.where(neg, -dirs, dirs)   # negation flips the sign bit, NaN too
     return adjusted

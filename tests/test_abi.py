@@ -186,3 +186,24 @@ def test_label26_validates_before_touching_the_gpu(lib):
     assert lib.m16_label26(fake, 0, 8, 8, fake, ctypes.byref(n), fake, nb, None) == N.M16_ERR_BAD_SHAPE
     assert lib.m16_label26(None, 8, 8, 8, fake, ctypes.byref(n), fake, nb, None) == N.M16_ERR_BAD_ARG
     assert lib.m16_label26(fake, 8, 8, 8, fake, ctypes.byref(n), fake, nb - 1, None) == N.M16_ERR_WORKSPACE
+
+
+def test_host_tree_helpers(lib):
+    """m16_tree_order / m16_compose_signs are host code: they run without a GPU."""
+    from miccai2016_gb300 import _native as N
+    import numpy as np
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    # forest: 0-1-2, 3-4; root 2
+    ea = np.array([0, 1, 3], np.int32)
+    eb = np.array([1, 2, 4], np.int32)
+    order = np.empty(5, np.int32)
+    pred = np.empty(5, np.int32)
+    assert lib.m16_tree_order(5, vp(ea), vp(eb), 3, 2, vp(order), vp(pred)) == N.M16_OK
+    assert order.tolist() == [2, 1, 0, 3, 4] and pred.tolist() == [1, 2, -1, -1, 3]
+    e = np.array([-1, 1, 0, 0, 2], np.int8)
+    s = np.zeros(5, np.int8)
+    assert lib.m16_compose_signs(5, vp(order), 5, vp(pred), vp(e), vp(s)) == N.M16_OK
+    assert s.tolist() == [-1, 1, 1, 1, -1]
+    bad = np.array([0, 7], np.int32)
+    assert lib.m16_tree_order(5, vp(bad), vp(bad), 2, 0, vp(order), vp(pred)) == N.M16_ERR_BAD_ARG
+    assert lib.m16_tree_order(5, vp(ea), vp(eb), 3, 9, vp(order), vp(pred)) == N.M16_ERR_BAD_ARG
