@@ -572,10 +572,12 @@ STAGE_BYTES = {
     "frangi": 72,          # per voxel-scale: image 4 read, Hessian 24 written + read, val 4 + 4, quat 12
     "detect_ridges": 20,   # per voxel: response 4 + quaternion 12 read, ridge 4 written
     "extract_main_dirs": 24,        # per voxel: quaternion 12 read, direction 12 written
+    "detect_ridges_main_dirs": 32,  # both in one pass: response 4 + quaternion 12 read, ridge 4 + direction 12 written
     "gvf": 40,             # per voxel-iteration: g 12, v 12, r 4 read; g 12 written
     "complete_transformations": 24,  # per voxel: direction 12 read, quaternion 12 written
 }
-STAGES = ["frangi", "detect_ridges", "extract_main_dirs", "adjust_nonridge_signs", "gvf", "complete_transformations"]
+STAGES = ["frangi", "detect_ridges", "extract_main_dirs", "detect_ridges_main_dirs", "adjust_nonridge_signs", "gvf",
+          "complete_transformations"]
 
 
 def run_stages(args, cfg):
@@ -663,6 +665,14 @@ def run_stages(args, cfg):
     dirs = torch.empty_like(quat)
     stage("extract_main_dirs", lambda: N.check("m16_extract_main_directions", L.m16_extract_main_directions(
         N.ptr(quat), n, N.ptr(dirs), sp)), n, "voxels", STAGE_BYTES["extract_main_dirs"])
+
+    dirs2 = torch.empty_like(quat)
+    stage("detect_ridges_main_dirs", lambda: N.check("m16_detect_ridges_main_directions",
+                                                     L.m16_detect_ridges_main_directions(
+                                                         N.ptr(resp), N.ptr(quat), d0, d1, d2, 0.01, N.ptr(ridge),
+                                                         N.ptr(dirs2), sp)),
+          n, "voxels", STAGE_BYTES["detect_ridges_main_dirs"])
+    del dirs2
 
     # the ridge list of the host steps (hysteresis, MST, cleaning), then the GPU sign flip
     work = dirs.clone()

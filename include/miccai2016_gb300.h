@@ -355,6 +355,15 @@ int m16_eigs(const float *h6, int64_t n, float *out6, void *stream);
 int m16_detect_ridges(const float *resp, const float *quat3, int32_t d0, int32_t d1, int32_t d2,
                       double threshold, float *ridge, void *stream);
 
+/* m16_detect_ridges and m16_extract_main_directions in one pass over the
+ * quaternions (their double-precision expansion is evaluated once): ridge
+ * (N) and dirs3 (N x 3) as the two calls give them.  dirs3 may be quat3 (each
+ * voxel reads only its own quaternion).  d0 <= 65535.  Replaces the pair
+ * RawRidgeDetector.execute + AdvancedAdjuster._qeigs_to_main_dirs
+ * (ridge_detection.py:45-77, adjust_directions.py:341-362). */
+int m16_detect_ridges_main_directions(const float *resp, const float *quat3, int32_t d0, int32_t d1, int32_t d2,
+                                      double threshold, float *ridge, float *dirs3, void *stream);
+
 /* Main direction (first eigenvector column) of each squeezed quaternion,
  * replacing extractMainDirections (adjust_directions.cl:29-43) as used by
  * AdvancedAdjuster._qeigs_to_main_dirs (adjust_directions.py:341-362).

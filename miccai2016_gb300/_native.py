@@ -113,6 +113,8 @@ def _declare(L):
     L.m16_eigs.argtypes = [_vp, _i64, _vp, _vp]
     L.m16_detect_ridges.restype = ctypes.c_int
     L.m16_detect_ridges.argtypes = [_vp, _vp, _i32, _i32, _i32, _f64, _vp, _vp]
+    L.m16_detect_ridges_main_directions.restype = ctypes.c_int
+    L.m16_detect_ridges_main_directions.argtypes = [_vp, _vp, _i32, _i32, _i32, _f64, _vp, _vp, _vp]
     L.m16_extract_main_directions.restype = ctypes.c_int
     L.m16_extract_main_directions.argtypes = [_vp, _i64, _vp, _vp]
     L.m16_complete_transformations.restype = ctypes.c_int

@@ -152,13 +152,25 @@ class AdvancedAdjuster(TreePrintable):
             if not self.ridge_detection_only:
                 adjusted = self._adjust_all_directions(ridge_coords, ridge_dirs)
         del self._d_qeigs
+        self._d_main = None
         torch.cuda.current_stream().synchronize()
         return adjusted
 
     def _label_ridge(self):
-        """adjust_directions.py:258-288"""
-        ridge = self._ridge_detector.detect(self.response, self._d_qeigs)
-        ridge = np.require(ridge, np.float32, ["C", "A", "W"])
+        """adjust_directions.py:258-288.  The ridge candidates and the main
+        directions come from one pass over the quaternions
+        (m16_detect_ridges_main_directions); the directions are kept on the
+        device for _qeigs_to_main_dirs."""
+        torch = N.torch_mod()
+        shape = tuple(int(v) for v in self.response.shape)
+        resp = N.to_device_f32(self.response, shape)
+        d_ridge = torch.empty(shape, dtype=torch.float32, device=N.device())
+        self._d_main = torch.empty_like(self._d_qeigs)
+        st = N.lib().m16_detect_ridges_main_directions(N.ptr(resp), N.ptr(self._d_qeigs), shape[0], shape[1],
+                                                      shape[2], float(self._ridge_detector.threshold),
+                                                      N.ptr(d_ridge), N.ptr(self._d_main), N.stream_ptr())
+        N.check("m16_detect_ridges_main_directions", st)
+        ridge = np.require(d_ridge.cpu().numpy(), np.float32, ["C", "A", "W"])
         if self._hysteresis:
             sure = np.logical_and(ridge, self.response >= self.threshold[1])
             ridge[:] = hysteresis_threshold(ridge, sure, labeler=self.labeler)
@@ -191,9 +203,14 @@ class AdvancedAdjuster(TreePrintable):
     def _qeigs_to_main_dirs(self):
         """adjust_directions.py:341-362: the device quaternion buffer is
         overwritten with the main directions, which are also returned."""
-        n = self._d_qeigs.numel() // 3
-        st = N.lib().m16_extract_main_directions(N.ptr(self._d_qeigs), n, N.ptr(self._d_qeigs), N.stream_ptr())
-        N.check("m16_extract_main_directions", st)
+        if getattr(self, "_d_main", None) is not None:   # computed with the ridge candidates
+            self._d_qeigs.copy_(self._d_main)
+            self._d_main = None
+        else:
+            n = self._d_qeigs.numel() // 3
+            st = N.lib().m16_extract_main_directions(N.ptr(self._d_qeigs), n, N.ptr(self._d_qeigs),
+                                                     N.stream_ptr())
+            N.check("m16_extract_main_directions", st)
         main_dirs = self._d_qeigs.cpu().numpy()
         self.__main_dirs_unadjusted = main_dirs.copy()
         return main_dirs

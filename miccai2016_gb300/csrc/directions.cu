@@ -67,19 +67,27 @@ __device__ __forceinline__ void quat_cols(const float q[4], float c0[3], float c
 }
 
 // ---- detectRidges -----------------------------------------------------------
+// dirs3 (optional): the main direction (first column) of the same expansion,
+// what extractMainDirections computes, written in the same pass
 __global__ void __launch_bounds__(kBX * kBY) dr_detect_ridges_kernel(const float *__restrict__ resp,
                                                                      const float *__restrict__ quat3,
                                                                      float *__restrict__ ridge, int d0, int d1,
-                                                                     int d2, double threshold)
+                                                                     int d2, double threshold,
+                                                                     float *__restrict__ dirs3)
 {
     const int x = blockIdx.x * kBX + threadIdx.x;
     const int y = blockIdx.y * kBY + threadIdx.y;
     const int z = blockIdx.z;
     if (x >= d2 || y >= d1) return;
     const int64_t i = ((int64_t)z * d1 + y) * d2 + x;
-    float q[4], c1[3], c2[3];
+    float q[4], c0[3], c1[3], c2[3];
     qexpand_ref(quat3[3 * i], quat3[3 * i + 1], quat3[3 * i + 2], q);
-    quat_cols(q, nullptr, c1, c2);
+    quat_cols(q, dirs3 ? c0 : nullptr, c1, c2);
+    if (dirs3) {
+        dirs3[3 * i] = c0[0];
+        dirs3[3 * i + 1] = c0[1];
+        dirs3[3 * i + 2] = c0[2];
+    }
     const float pos[3] = {(float)z, (float)y, (float)x};
     const int dims[3] = {d0, d1, d2};
     float maxv = -INFINITY;
@@ -520,7 +528,19 @@ extern "C" int m16_detect_ridges(const float *resp, const float *quat3, int32_t 
     if (!resp || !quat3 || !ridge) return M16_ERR_BAD_ARG;
     const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)d0);
     dr_detect_ridges_kernel<<<grid, dim3(kBX, kBY, 1), 0, (cudaStream_t)stream>>>(resp, quat3, ridge, d0, d1, d2,
-                                                                                 threshold);
+                                                                                 threshold, nullptr);
+    M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}
+
+extern "C" int m16_detect_ridges_main_directions(const float *resp, const float *quat3, int32_t d0, int32_t d1,
+                                                 int32_t d2, double threshold, float *ridge, float *dirs3, void *stream)
+{
+    if (d0 < 1 || d1 < 1 || d2 < 1 || d0 > 65535) return M16_ERR_BAD_SHAPE;
+    if (!resp || !quat3 || !ridge || !dirs3) return M16_ERR_BAD_ARG;
+    const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)d0);
+    dr_detect_ridges_kernel<<<grid, dim3(kBX, kBY, 1), 0, (cudaStream_t)stream>>>(resp, quat3, ridge, d0, d1, d2,
+                                                                                 threshold, dirs3);
     M16_CUDA_TRY(cudaGetLastError());
     return M16_OK;
 }

@@ -153,3 +153,25 @@ def test_completer_round_trip_keeps_the_main_direction():
     back = _gpu_extract(q)
     vn = v / np.linalg.norm(v, axis=-1, keepdims=True)
     assert np.max(np.abs(back - vn)) <= 1e-5
+
+
+@pytest.mark.parametrize("shape", [(40, 33, 50), (1, 20, 20)])
+def test_fused_ridges_and_main_directions_equal_the_two_calls(shape):
+    import torch
+    from miccai2016_gb300 import _native as N
+    from miccai2016_gb300.ridge_detection import RawRidgeDetector
+    rng = np.random.RandomState(sum(shape) + 1)
+    resp = rng.uniform(0, 1, shape).astype(np.float32)
+    q = I.random_squeezed(rng, shape)
+    ridge = RawRidgeDetector(None, 0.05).detect(resp, q)
+    main = _gpu_extract(q)
+    d_resp = torch.from_numpy(resp).cuda()
+    for in_place in (False, True):
+        d_q = torch.from_numpy(np.ascontiguousarray(q)).cuda()
+        d_ridge = torch.empty(shape, dtype=torch.float32, device="cuda")
+        d_dirs = d_q if in_place else torch.empty_like(d_q)
+        st = N.lib().m16_detect_ridges_main_directions(N.ptr(d_resp), N.ptr(d_q), *shape, 0.05, N.ptr(d_ridge),
+                                                      N.ptr(d_dirs), N.stream_ptr())
+        N.check("m16_detect_ridges_main_directions", st)
+        assert np.array_equal(d_ridge.cpu().numpy(), ridge)
+        assert np.array_equal(_bits(d_dirs.cpu().numpy()), _bits(main))
