@@ -31,7 +31,7 @@ import itertools
 
 import numpy as np
 import scipy.sparse
-from scipy.sparse.csgraph import connected_components, minimum_spanning_tree
+from scipy.sparse.csgraph import minimum_spanning_tree
 from scipy.spatial import cKDTree
 
 from . import _native as N
@@ -121,6 +121,25 @@ def _local_mst_gpu(pts, vs, r, offsets):
     return e[:, 0], e[:, 1]
 
 
+def forest_components(n, ea, eb):
+    """(count, component of each point) of the forest with edges (ea, eb) on
+    points 0..n-1, numbered in the order of each component's lowest index --
+    the numbering of scipy.sparse.csgraph.connected_components.  The
+    components come from the library's traversal (m16_tree_order): it starts
+    a new tree at each point not yet reached, in index order."""
+    L = N.lib()
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    a32 = np.ascontiguousarray(ea, dtype=np.int32)
+    b32 = np.ascontiguousarray(eb, dtype=np.int32)
+    order = np.empty(n, np.int32)
+    pred = np.empty(n, np.int32)
+    N.check("m16_tree_order", L.m16_tree_order(n, vp(a32), vp(b32), len(a32), 0, vp(order), vp(pred)))
+    starts = pred[order] < 0
+    comp = np.empty(n, np.int64)
+    comp[order] = np.cumsum(starts) - 1
+    return int(np.count_nonzero(starts)), comp
+
+
 def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, local="gpu"):
     """Edges (a, b) of the (weight, i, j)-ordered Euclidean MST of integer
     points (R x 3, axis order 0, 1, 2, distinct) with per-axis voxel size.
@@ -143,30 +162,35 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, lo
     else:
         raise ValueError("local must be 'gpu' or 'host'")
     # global phase: join the local trees
-    forest = scipy.sparse.coo_matrix((np.ones(len(ta)), (ta, tb)), shape=(R, R))
-    ncomp, comp = connected_components(forest, directed=False)
+    ncomp, comp = forest_components(R, ta, tb)
     if ncomp == 1 or not join_components:
         return ta, tb
-    members = [np.nonzero(comp == c)[0] for c in range(ncomp)]
-    trees = [cKDTree(u[m]) for m in members]
+    by_comp = np.argsort(comp, kind="stable")   # each component's points in index order
+    members = np.split(by_comp, np.cumsum(np.bincount(comp, minlength=ncomp))[:-1])
+    trees = {}
+
+    def tree(c):
+        # kd-trees only find candidates (their queries are exact); the
+        # sliding-midpoint build is the fastest one
+        if c not in trees:
+            trees[c] = cKDTree(u[members[c]], balanced_tree=False, compact_nodes=False)
+        return trees[c]
+
     ci, cj, cw, ca, cb = [], [], [], [], []
     for A in range(ncomp):
-        mA = members[A]
         for B in range(A + 1, ncomp):
-            mB = members[B]
-            # nearest point of A for each point of B, then every pair at that
-            # distance, so ties resolve by (i, j)
-            dist, _ = trees[A].query(u[mB], k=1)
+            # the smaller tree's points are queried against the larger one:
+            # nearest point for each, then every pair at the least distance,
+            # so ties resolve by (i, j)
+            S, Lg = (A, B) if len(members[A]) <= len(members[B]) else (B, A)
+            mS, mL = members[S], members[Lg]
+            dist, _ = tree(Lg).query(u[mS], k=1)
             dmin = float(np.min(dist))
-            cand = trees[A].query_ball_point(u[mB], dmin * (1 + 1e-9) + 1e-12)
-            pa, pb = [], []
-            for kb, lst in enumerate(cand):
-                for ka in lst:
-                    pa.append(mA[ka])
-                    pb.append(mB[kb])
-            pa = np.asarray(pa, np.int64)
-            pb = np.asarray(pb, np.int64)
-            lo_, hi_ = np.minimum(pa, pb), np.maximum(pa, pb)
+            near = np.nonzero(dist <= dmin * (1 + 1e-9) + 1e-12)[0]
+            cand = tree(Lg).query_ball_point(u[mS[near]], dmin * (1 + 1e-9) + 1e-12)
+            ps = np.repeat(mS[near], [len(lst) for lst in cand])
+            pl = mL[np.fromiter(itertools.chain.from_iterable(cand), np.int64)]
+            lo_, hi_ = np.minimum(ps, pl), np.maximum(ps, pl)
             ww = _weights(u, lo_, hi_)
             best = np.lexsort((hi_, lo_, ww))[0]
             ci.append(A); cj.append(B); cw.append(ww[best]); ca.append(lo_[best]); cb.append(hi_[best])

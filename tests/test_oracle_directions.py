@@ -97,6 +97,43 @@ def test_sparse_mst_equals_the_dense_stable_kruskal(vs):
                                                                        np.maximum(t.row, t.col)))
 
 
+@pytest.mark.parametrize("vs", [(1, 1, 1), (1, 1, 2.5)])
+def test_join_of_one_large_and_many_small_trees_equals_the_dense_stable_kruskal(vs):
+    """Trees of very different sizes, in index orders that put the large one
+    first, last and in between: the join queries the smaller tree of every
+    pair against the larger one."""
+    from miccai2016_gb300.ridge_mst import ridge_mst_edges
+    rng = np.random.RandomState(7)
+    for t in range(3):
+        big = np.argwhere(np.ones((9, 9, 6), bool))
+        small = [rng.randint(0, 3, (rng.randint(1, 5), 3)) + rng.randint(-12, 24, 3) for _ in range(12)]
+        pts = np.unique(np.concatenate([big] + small), axis=0)
+        order = [rng.permutation(len(pts)), np.argsort(-np.abs(pts).sum(1), kind="stable"),
+                 np.argsort(np.abs(pts - 4).sum(1), kind="stable")][t]
+        pts = pts[order]
+        a, b = ridge_mst_edges(pts, vs, local="host")
+        ref = A.stable_mst(pts, vs).tocoo()
+        assert set(zip(np.minimum(a, b), np.maximum(a, b))) == set(zip(np.minimum(ref.row, ref.col),
+                                                                       np.maximum(ref.row, ref.col)))
+
+
+def test_forest_components_number_like_scipy():
+    import scipy.sparse
+    from scipy.sparse.csgraph import connected_components
+    from miccai2016_gb300.ridge_mst import forest_components
+    rng = np.random.RandomState(8)
+    n = 500
+    p = rng.permutation(n)
+    a, b = [], []
+    for k in range(1, n):
+        if rng.uniform() < 0.9:   # a random forest: each point hangs off an earlier one, or starts a tree
+            a.append(p[k]); b.append(p[rng.randint(0, k)])
+    a, b = np.asarray(a), np.asarray(b)
+    n1, c1 = forest_components(n, a, b)
+    n2, c2 = connected_components(scipy.sparse.coo_matrix((np.ones(len(a)), (a, b)), shape=(n, n)), directed=False)
+    assert n1 == n2 and np.array_equal(c1, c2)
+
+
 def test_ridge_directions_and_cleaning_match_the_reference_logic():
     from miccai2016_gb300.adjust_directions import AdvancedAdjuster
     rng = np.random.RandomState(4)
