@@ -230,10 +230,12 @@ def _u_buffer(torch, shape):
     return torch.empty(shape, dtype=torch.float32).pin_memory()
 
 
-def run_served(server, payloads, requests, max_resident=None):
+def run_served(server, payloads, requests, max_resident=None, keep=None):
     """Replay the arrivals in real time through the server.  Returns per-tag
     dict of arrival, completion (s from the start), iterations, residual and
-    the host u."""
+    the host u.  With keep set, only requests with tag < keep keep their u;
+    the others' pinned buffers go back to the host allocator's cache when they
+    finish, so long runs hold a bounded amount of host memory."""
     import torch
     pending = deque(sorted(requests, key=lambda r: r["arrival"]))
     waiting = deque()
@@ -267,14 +269,17 @@ def run_served(server, payloads, requests, max_resident=None):
             time.sleep(0.0002)   # only downloads in flight
         for tag, it, res in server.poll():
             out[tag].update(done=time.perf_counter() - t0, iterations=it, residual=res)
+            if keep is not None and tag >= keep:
+                del out[tag]["u"]
             resident -= 1
             finished += 1
     return out
 
 
-def run_plain(payloads, requests, num_iter=3000, update=30, error_bound=1e-4):
+def run_plain(payloads, requests, num_iter=3000, update=30, error_bound=1e-4, keep=None):
     """The same arrivals served one request at a time by the drop-in
-    CmfCutQAnisotropicGpu (inputs from the host, u back to the host)."""
+    CmfCutQAnisotropicGpu (inputs from the host, u back to the host).  keep
+    as in run_served."""
     import torch
     from .continuous_cut_anisotropic_gpu import CmfCutQAnisotropicGpu
     p = CmfCutQAnisotropicGpu.CutParameters()
@@ -296,6 +301,8 @@ def run_plain(payloads, requests, num_iter=3000, update=30, error_bound=1e-4):
                              iterations=cutter.last_iterations,
                              residual=float(cutter.last_residuals[-1]) if len(cutter.last_residuals) else float("nan"),
                              u=uh)
+        if keep is not None and r["tag"] >= keep:
+            del out[r["tag"]]["u"], uh
     return out
 
 
@@ -318,11 +325,11 @@ def served_vs_plain(n_requests=96, rate=50.0, pool=8, seed=0, max_resident=None,
     run_served(srv, payloads, warm)
     run_plain(payloads, warm)
     torch.cuda.synchronize()
-    served = run_served(srv, payloads, reqs, max_resident=max_resident)
+    served = run_served(srv, payloads, reqs, max_resident=max_resident, keep=check)
     info = srv.info()
     srv.close()
     torch.cuda.synchronize()
-    plain = run_plain(payloads, reqs)
+    plain = run_plain(payloads, reqs, keep=check)
     diffs, itdiff = [], []
     for t in range(min(check, n_requests)):
         diffs.append(float(np.max(np.abs(served[t]["u"].numpy() - plain[t]["u"].numpy()))))
