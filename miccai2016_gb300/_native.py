@@ -50,7 +50,7 @@ class CutParams(ctypes.Structure):
 
 
 # iteration paths of the single solve (m16_solve_stats.path)
-PATH_DEFAULT, PATH_TWO_SWEEPS, PATH_FUSED = 0, 1, 2
+PATH_DEFAULT, PATH_TWO_SWEEPS, PATH_FUSED, PATH_PAIRS = 0, 1, 2, 3
 
 
 BATCH_NO_GRAPH = 1   # m16_solve_stats.flags
@@ -61,7 +61,8 @@ class SolveStats(ctypes.Structure):
     """m16_solve_stats (include/miccai2016_gb300.h)."""
     _fields_ = [("time_kernels", _i32), ("launches", _i32), ("p_launches", _i32), ("u_launches", _i32),
                 ("p_ms", _f64), ("u_ms", _f64), ("path", _i32), ("flags", _i32),
-                ("blocks_per_sm", _i32), ("reserved", _i32)]
+                ("blocks_per_sm", _i32), ("pair_launches", _i32), ("pair_ms", _f64), ("pair_zc", _i32),
+                ("reserved", _i32)]
 
 
 class BatchVolume(ctypes.Structure):

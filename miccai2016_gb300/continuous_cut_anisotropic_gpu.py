@@ -53,9 +53,13 @@ class CmfCutQAnisotropicGpu(TreePrintable):
         self.last_iterations = None
         self.last_residuals = None
         self._ws = None
-        # how an iteration is launched (N.PATH_DEFAULT, PATH_TWO_SWEEPS or
-        # PATH_FUSED); the paths give the same result within float rounding
+        # how an iteration is launched (N.PATH_DEFAULT, PATH_TWO_SWEEPS,
+        # PATH_FUSED or PATH_PAIRS); the paths give the same result within
+        # float rounding
         self.iteration_path = N.PATH_DEFAULT
+        # z-planes per block of the two-iteration launches (0: the library's choice)
+        self.pair_zc = 0
+        self.last_stats = None
 
     # -- reference: execute() with its exception-forwarding wrapper (:143-196)
     def execute(self, img, quats, eigs, alpha, cs, ct, labels=None, scaling=None, verbose=True):
@@ -128,12 +132,14 @@ class CmfCutQAnisotropicGpu(TreePrintable):
         iters = ctypes.c_int32(0)
         nres = ctypes.c_int32(0)
         stats = N.SolveStats(0, 0, 0, 0, 0.0, 0.0, int(self.iteration_path), 0)
+        stats.pair_zc = int(self.pair_zc)
         st = L.m16_maxflow_solve_ex(N.ptr(d_img), N.ptr(d_q), sqc, N.ptr(sqp), N.ptr(d_alpha), alpha_scalar,
                                     N.ptr(d_cs), N.ptr(d_ct), N.ptr(d_lab), shape[0], shape[1], shape[2],
                                     ctypes.byref(cp), N.ptr(u), ctypes.byref(iters), resid, cap,
                                     ctypes.byref(nres), N.ptr(self._ws), self._ws.numel(), N.stream_ptr(),
                                     ctypes.byref(stats))
         N.check("m16_maxflow_solve_ex", st)
+        self.last_stats = stats
         self.last_iterations = int(iters.value)
         self.last_residuals = np.array(resid[:min(nres.value, cap)], dtype=np.float64)
         if verbose:

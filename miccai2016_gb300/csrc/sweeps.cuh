@@ -53,6 +53,59 @@ struct LabelView {
     float *pt, *u, *tmp;
 };
 
+// P at one voxel (update_qp.cl:150-232): g = steps * grad tmp from the
+// voxel's tmp (tc) and its forward neighbours (tz, ty, tx; each used only
+// where its flag says the neighbour exists), p = H^-1 hp + H^T g projected
+// onto |p| <= rad, returns hp = H p.  (s0v, s1v, s2v) = sqrt of the
+// eigenvalues, (i0v, i1v, i2v) their reciprocals.
+__device__ __forceinline__ float3 flow_point(float ss0, float ss1, float ss2, float tc, float tz, float ty, float tx,
+                                             bool zin, bool yin, bool xin, float4 q, float rad, float h0, float h1,
+                                             float h2, float s0v, float s1v, float s2v, float i0v, float i1v,
+                                             float i2v)
+{
+    const float3 g = make_float3(zin ? (tz - tc) * ss0 : 0.f, yin ? (ty - tc) * ss1 : 0.f,
+                                 xin ? (tx - tc) * ss2 : 0.f);
+    const Rot R = quat2rot(q);
+    const float3 rg = rot_t(R, g);
+    const float3 rh = rot_t(R, make_float3(h0, h1, h2));
+    float3 p = make_float3(rh.x * i0v + rg.x * s0v, rh.y * i1v + rg.y * s1v, rh.z * i2v + rg.z * s2v);
+    const float nrm = sqrtf(p.x * p.x + p.y * p.y + p.z * p.z);
+    const float sc = nrm > rad ? rad / nrm : 1.f;
+    p = make_float3(p.x * sc * s0v, p.y * sc * s1v, p.z * sc * s2v);
+    return rot(R, p);
+}
+
+// U at one voxel (update_qp.cl:241-300 with update_tmp :311-316 fused):
+// div(hp) from the voxel's hp (h0, h1, h2) and its backward neighbours'
+// (h0m, h1m, h2m; z only where zlo, the own component only where the forward
+// flag is set), then p_s, p_t, u and tmp = err - u / cc.  Returns err.
+// p_s = min(div + p_t - (u - s_off)/cc, C_s); p_t = min(-div + p_s + (u - t_off)/cc, C_t)
+// with (s_off, t_off) = (1, 0) unsupervised and (!(l & 2), l & 1) with seeds l.
+template <bool SUPERVISED>
+__device__ __forceinline__ float label_point(float rcc, float rs0, float rs1, float rs2, float h0, float h1, float h2,
+                                             float h0m, float h1m, float h2m, bool zlo, bool zhi, bool yhi, bool xhi,
+                                             float uo, float ptv, float csv, float ctv, uint8_t lab, float &ptn,
+                                             float &un, float &tmpv)
+{
+    const float a0 = (zhi ? h0 : 0.f) - (zlo ? h0m : 0.f);
+    const float a1 = (yhi ? h1 : 0.f) - h1m;
+    const float a2 = (xhi ? h2 : 0.f) - h2m;
+    const float div = a0 * rs0 + a1 * rs1 + a2 * rs2;
+    float s_off = 1.f, t_off = 0.f;
+    if (SUPERVISED) {
+        s_off = (float)(!(lab & 2));
+        t_off = (float)(lab & 1);
+    }
+    const float psx = div + ptv - rcc * (uo - s_off);
+    const float ps = csv < psx ? csv : psx;
+    const float ptx = -div + ps + rcc * (uo - t_off);
+    ptn = ctv < ptx ? ctv : ptx;
+    const float err = div - ps + ptn;
+    un = uo - err / rcc;
+    tmpv = err - un * rcc;
+    return err;
+}
+
 // P: p = H^-1 hp + H^T (steps grad tmp), projected onto |p| <= alpha, hp = H p
 // (update_qp.cl:150-232) for voxels (z0..z1, y, x).
 template <bool POINTWISE, int ALPHA>
@@ -93,23 +146,14 @@ __device__ __forceinline__ void flow_column(const FlowView &a, int x, int y, int
                 const int64_t j = i + k * s0;
                 const float tc = k == 0 ? t : tz[k - 1];
                 const bool zin = zb + k < a.d0 - 1;
-                const float3 g = make_float3(zin ? (tz[k] - tc) * a.ss0 : 0.f, yin ? (ty[k] - tc) * a.ss1 : 0.f,
-                                             xin ? (tx[k] - tc) * a.ss2 : 0.f);
-                const Rot R = quat2rot(q[k]);
                 float s0v = a.sq0, s1v = a.sq1, s2v = a.sq2, i0v = a.isq0, i1v = a.isq1, i2v = a.isq2;
                 if (POINTWISE) {
                     s0v = se0[k]; s1v = se1[k]; s2v = se2[k];
                     i0v = 1.f / s0v; i1v = 1.f / s1v; i2v = 1.f / s2v;
                 }
                 const float rad = ALPHA == kAlphaFromGrad2 ? a.w * expf(a.neg_inv_decay2 * al[k]) : al[k];
-                const float3 rg = rot_t(R, g);
-                const float3 rh = rot_t(R, make_float3(h0[k], h1[k], h2[k]));
-                float3 p = make_float3(rh.x * i0v + rg.x * s0v, rh.y * i1v + rg.y * s1v,
-                                       rh.z * i2v + rg.z * s2v);
-                const float nrm = sqrtf(p.x * p.x + p.y * p.y + p.z * p.z);
-                const float sc = nrm > rad ? rad / nrm : 1.f;
-                p = make_float3(p.x * sc * s0v, p.y * sc * s1v, p.z * sc * s2v);
-                const float3 h = rot(R, p);
+                const float3 h = flow_point(a.ss0, a.ss1, a.ss2, tc, tz[k], ty[k], tx[k], zin, yin, xin, q[k], rad,
+                                            h0[k], h1[k], h2[k], s0v, s1v, s2v, i0v, i1v, i2v);
                 a.hp0[j] = h.x;
                 a.hp1[j] = h.y;
                 a.hp2[j] = h.z;
@@ -155,26 +199,14 @@ __device__ __forceinline__ float label_column(const LabelView &a, int x, int y, 
                 const int64_t j = i + k * s0;
                 const int z = zb + k;
                 const float prev0 = k == 0 ? h0m : h0[k - 1];
-                const float a0 = (z < a.d0 - 1 ? h0[k] : 0.f) - (z > 0 ? prev0 : 0.f);
-                const float a1 = (yhi ? h1[k] : 0.f) - h1m[k];
-                const float a2 = (xhi ? h2[k] : 0.f) - h2m[k];
-                const float div = a0 * a.rs0 + a1 * a.rs1 + a2 * a.rs2;
-                // p_s = min(div + p_t - (u - s_off)/cc, C_s); p_t = min(-div + p_s + (u - t_off)/cc, C_t)
-                // with (s_off, t_off) = (1, 0) unsupervised and (!(l & 2), l & 1) with seeds l
-                float s_off = 1.f, t_off = 0.f;
-                if (SUPERVISED) {
-                    s_off = (float)(!(lab[k] & 2));
-                    t_off = (float)(lab[k] & 1);
-                }
-                const float psx = div + ptv[k] - a.rcc * (uo[k] - s_off);
-                const float ps = csv[k] < psx ? csv[k] : psx;
-                const float ptx = -div + ps + a.rcc * (uo[k] - t_off);
-                const float ptn = ctv[k] < ptx ? ctv[k] : ptx;
-                const float err = div - ps + ptn;
-                const float un = uo[k] - err / a.rcc;
+                float ptn, un, tmpv;
+                const float err = label_point<SUPERVISED>(a.rcc, a.rs0, a.rs1, a.rs2, h0[k], h1[k], h2[k], prev0,
+                                                          h1m[k], h2m[k], z > 0, z < a.d0 - 1, yhi, xhi, uo[k],
+                                                          ptv[k], csv[k], ctv[k], SUPERVISED ? lab[k] : (uint8_t)0,
+                                                          ptn, un, tmpv);
                 a.pt[j] = ptn;
                 a.u[j] = un;
-                a.tmp[j] = err - un * a.rcc;
+                a.tmp[j] = tmpv;
                 acc += fabsf(err);
             }
         }

@@ -84,7 +84,7 @@ def test_solve_ex_rejects_an_unknown_iteration_path(lib):
     it = ctypes.c_int32(0)
     sq = (ctypes.c_double * 3)(1, 1, 1)
     fake = ctypes.c_void_p(256)
-    for path in (-1, 3):
+    for path in (-1, 4):
         s = N.SolveStats(0, 0, 0, 0, 0.0, 0.0, path, 0)
         st = lib.m16_maxflow_solve_ex(fake, fake, sq, None, None, 0.1, fake, fake, None, 4, 4, 4, ctypes.byref(p),
                                       fake, ctypes.byref(it), None, 0, None, fake, 1 << 20, None, ctypes.byref(s))
