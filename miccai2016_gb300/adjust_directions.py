@@ -182,8 +182,10 @@ class AdvancedAdjuster(TreePrintable):
         directions are longest (adjust_directions.py:290-339).  Per segment the
         directions are summed in the reference's order (C order of the voxels)."""
         scaled = ridge_dirs * self.__voxel_size   # float32 * tuple -> float64, as in the reference
-        components = label26(labeled_ridge, where=self.labeler)[0]
-        labels = np.unique(components)[1:]
+        components, n_lab = label26(labeled_ridge, where=self.labeler)
+        # np.unique(components)[1:] without the sort: the labels are 1..n_lab,
+        # and "[1:]" drops label 1 too when no voxel is background
+        labels = np.arange(1 if len(ridge_coords) < components.size else 2, n_lab + 1)
         point_label = components[tuple(np.asarray(ridge_coords, np.intp).T)]
         order = np.argsort(point_label, kind="stable")
         sorted_labels = point_label[order]
@@ -196,7 +198,9 @@ class AdvancedAdjuster(TreePrintable):
         boundary = int(np.ceil(3 * np.log(np.e + len(ordered))))
         print("Keeping %s of %s labels." % (boundary, len(ordered)))
         kept = ordered[:boundary]
-        cleaned = np.isin(components, kept).astype(labeled_ridge.dtype).reshape(components.shape)
+        keep = np.zeros(n_lab + 1, dtype=bool)   # np.in1d(components, kept) as a table lookup
+        keep[np.asarray(kept, dtype=np.int64)] = True
+        cleaned = keep[components].astype(labeled_ridge.dtype).reshape(components.shape)
         self.__ridge = cleaned
         return cleaned
 

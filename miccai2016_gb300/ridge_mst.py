@@ -162,9 +162,9 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, lo
     else:
         raise ValueError("local must be 'gpu' or 'host'")
     # global phase: join the local trees
-    ncomp, comp = forest_components(R, ta, tb)
-    if ncomp == 1 or not join_components:
+    if not join_components or len(ta) == R - 1:   # not asked for, or already one tree
         return ta, tb
+    ncomp, comp = forest_components(R, ta, tb)
     by_comp = np.argsort(comp, kind="stable")   # each component's points in index order
     members = np.split(by_comp, np.cumsum(np.bincount(comp, minlength=ncomp))[:-1])
     trees = {}

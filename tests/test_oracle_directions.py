@@ -180,3 +180,20 @@ def test_cleaning_is_the_same_without_joining_the_segments():
     assert np.array_equal(k1, k2)
     # every point's direction is the joined one up to one sign per segment
     assert np.allclose(np.abs(d1), np.abs(d2))
+
+
+def test_cleaning_of_a_ridge_without_background_drops_label_one_like_the_reference():
+    """np.unique(components)[1:] drops label 1 when no voxel is background."""
+    from miccai2016_gb300.adjust_directions import AdvancedAdjuster
+    rng = np.random.RandomState(12)
+    shape = (3, 4, 5)
+    ridge = np.ones(shape, np.float32)
+    main = rng.normal(size=shape + (3,)).astype(np.float32)
+    obj = AdvancedAdjuster((0.01, 0.3), np.zeros(shape + (3,), np.float32), np.zeros(shape, np.float32))
+    obj.mst_local = "host"
+    obj.labeler = "host"
+    c, d = obj._adjust_ridge_directions(ridge, main)
+    with contextlib.redirect_stdout(io.StringIO()):
+        k1 = A.clean_ridge(ridge, c, d, (1.0, 1.0, 1.0))
+        k2 = obj._do_clean_ridge(ridge, c, d)
+    assert np.array_equal(k1, k2) and not k2.any()
