@@ -726,6 +726,73 @@ def run_stages(args, cfg):
     print(json.dumps(line), flush=True)
 
 
+def run_paths(args, cfg):
+    """The iteration paths of the single solve side by side on one workload:
+    two sweeps, the fused iteration and two iterations per launch (at the
+    default z-chunk and at those of --pair-zc), CUDA events around whole
+    solves and, in a second pass, around every launch.  Prints one JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    from miccai2016_gb300 import _native as N
+    from miccai2016_gb300 import phantom as P
+
+    L = N.lib()
+    inp = _inputs(cfg)
+    shape = cfg["shape"]
+    dev = torch.device("cuda", 0)
+    d = {k: torch.from_numpy(inp[k]).to(dev) for k in ("img", "quats", "alpha", "cs", "ct")}
+    u = torch.empty(shape, dtype=torch.float32, device=dev)
+    cp = N.CutParams(0.2, 0.11, -1.0, cfg["num_iter"], 30, (ctypes.c_double * 3)(1, 1, 1))
+    ws = N.workspace(L.m16_maxflow_workspace_bytes(shape[0], shape[1], shape[2], ctypes.byref(cp)))
+    sq = (ctypes.c_double * 3)(*np.sqrt(P.ATV_EIGS).tolist())
+    stream = torch.cuda.current_stream()
+
+    def solve(path, zc=0, timing=0):
+        s = N.SolveStats(timing, 0, 0, 0, 0.0, 0.0, path, 0)
+        s.pair_zc = zc
+        it = ctypes.c_int32(0)
+        st = L.m16_maxflow_solve_ex(N.ptr(d["img"]), N.ptr(d["quats"]), sq, None, N.ptr(d["alpha"]), 0.0,
+                                    N.ptr(d["cs"]), N.ptr(d["ct"]), None, shape[0], shape[1], shape[2],
+                                    ctypes.byref(cp), N.ptr(u), ctypes.byref(it), None, 0, None, N.ptr(ws),
+                                    ws.numel(), ctypes.c_void_p(stream.cuda_stream), ctypes.byref(s))
+        N.check("m16_maxflow_solve_ex", st)
+        return s
+
+    def timed(path, zc=0):
+        for _ in range(args.warmup):
+            solve(path, zc)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            s = solve(path, zc)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        k = solve(path, zc, timing=1)
+        return dict(ms_per_solve=e0.elapsed_time(e1) / args.steps, launches=s.launches,
+                    pair_launches=k.pair_launches, pair_zc=k.pair_zc, two_sweep_iterations=k.p_launches,
+                    pair_launch_ms=k.pair_ms / max(k.pair_launches, 1),
+                    flow_sweep_ms=k.p_ms / max(k.p_launches, 1), label_sweep_ms=k.u_ms / max(k.u_launches, 1))
+
+    wanted = set(args.paths.split(","))
+    out = {}
+    u_ref = None
+    if "two_sweeps" in wanted:
+        out["two_sweeps"] = timed(N.PATH_TWO_SWEEPS)
+        u_ref = u.clone()
+    if "fused" in wanted:
+        out["fused"] = timed(N.PATH_FUSED)
+    if "pairs" in wanted:
+        out["pairs"] = timed(N.PATH_PAIRS)
+        if u_ref is not None:
+            out["pairs"]["max_u_diff_vs_two_sweeps"] = float((u - u_ref).abs().max())
+        for zc in [int(v) for v in args.pair_zc.split(",") if v]:
+            out["pairs_zc%d" % zc] = timed(N.PATH_PAIRS, zc)
+    print(json.dumps({"workload": "iteration paths of one %s solve, %d iterations" % ("x".join(map(str, shape)),
+                                                                                       cfg["num_iter"]),
+                      "steps": args.steps, "warmup": args.warmup, "paths": out}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -744,7 +811,14 @@ def main():
                     help="serving comparison: at most this many requests resident at once (0: no limit)")
     ap.add_argument("--served-requests", type=int, default=96,
                     help="requests of the serving comparison (0 skips it)")
+    ap.add_argument("--paths", default="two_sweeps,fused,pairs",
+                    help="paths workloads: which iteration paths to time")
+    ap.add_argument("--pair-zc", default="",
+                    help="paths workloads: comma-separated z-chunks of the two-iteration launches to time too")
     args = ap.parse_args()
+    if args.workload.startswith("paths"):
+        run_paths(args, _workload("plain" + args.workload[len("paths"):]))
+        return
     if args.workload == "ragged":
         run_ragged(args)
         return
