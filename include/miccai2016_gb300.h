@@ -480,6 +480,36 @@ size_t m16_label26_workspace_bytes(int32_t d0, int32_t d1, int32_t d2);
 int m16_label26(const uint8_t *mask, int32_t d0, int32_t d1, int32_t d2, int32_t *labels, int32_t *n_labels,
                 void *workspace, size_t workspace_bytes, void *stream);
 
+/* Workspace bytes of m16_label (the same as m16_label26's). */
+size_t m16_label_workspace_bytes(int32_t d0, int32_t d1, int32_t d2);
+
+/*
+ * m16_label26 with a choice of connectivity: 26 (a 3 x 3 x 3 structure of
+ * ones) or 6 (scipy.ndimage.label's default cross).  The same numbering as
+ * scipy.ndimage.label with that structure.  Synchronizes `stream`.
+ */
+int m16_label(const uint8_t *mask, int32_t d0, int32_t d1, int32_t d2, int32_t connectivity, int32_t *labels,
+              int32_t *n_labels, void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---- Dice of the largest connected component ---------------------------------------- */
+
+/* Workspace bytes of m16_dice_largest (0 for invalid sizes). */
+size_t m16_dice_largest_workspace_bytes(int32_t d0, int32_t d1, int32_t d2);
+
+/*
+ * The experiment's Dice (phantom_experiment.py:52-103, select_largest and
+ * dice_for): seg >= threshold, its 6-connected components, the largest one
+ * (the lowest label among equal sizes), then 2 |largest & truth| /
+ * (|largest| + |truth|) in double.  seg: float32 (device); truth: uint8
+ * (device), nonzero = inside.  dice, largest_size, n_components: host
+ * (largest_size and n_components may be NULL).  With no foreground the Dice
+ * is 0 and largest_size 0 (the reference fails there).  d0 * d1 * d2 < 2^31 - 1.
+ * Synchronizes `stream`.
+ */
+int m16_dice_largest(const float *seg, const uint8_t *truth, int32_t d0, int32_t d1, int32_t d2, float threshold,
+                     double *dice, int64_t *largest_size, int32_t *n_components, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
 /* ---- per-volume cut inputs and scoring --------------------------------------- */
 
 /*

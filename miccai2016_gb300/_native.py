@@ -130,6 +130,15 @@ def _declare(L):
     L.m16_label26_workspace_bytes.argtypes = [_i32, _i32, _i32]
     L.m16_label26.restype = ctypes.c_int
     L.m16_label26.argtypes = [_vp, _i32, _i32, _i32, _vp, ctypes.POINTER(_i32), _vp, _sz, _vp]
+    L.m16_label_workspace_bytes.restype = _sz
+    L.m16_label_workspace_bytes.argtypes = [_i32, _i32, _i32]
+    L.m16_label.restype = ctypes.c_int
+    L.m16_label.argtypes = [_vp, _i32, _i32, _i32, _i32, _vp, ctypes.POINTER(_i32), _vp, _sz, _vp]
+    L.m16_dice_largest_workspace_bytes.restype = _sz
+    L.m16_dice_largest_workspace_bytes.argtypes = [_i32, _i32, _i32]
+    L.m16_dice_largest.restype = ctypes.c_int
+    L.m16_dice_largest.argtypes = [_vp, _vp, _i32, _i32, _i32, ctypes.c_float, ctypes.POINTER(_f64),
+                                   ctypes.POINTER(_i64), ctypes.POINTER(_i32), _vp, _sz, _vp]
     L.m16_ridge_mst_workspace_bytes.restype = _sz
     L.m16_ridge_mst_workspace_bytes.argtypes = [_i64, _vp, _i32]
     L.m16_ridge_mst_local.restype = ctypes.c_int

@@ -186,6 +186,24 @@ def test_label26_validates_before_touching_the_gpu(lib):
     assert lib.m16_label26(fake, 0, 8, 8, fake, ctypes.byref(n), fake, nb, None) == N.M16_ERR_BAD_SHAPE
     assert lib.m16_label26(None, 8, 8, 8, fake, ctypes.byref(n), fake, nb, None) == N.M16_ERR_BAD_ARG
     assert lib.m16_label26(fake, 8, 8, 8, fake, ctypes.byref(n), fake, nb - 1, None) == N.M16_ERR_WORKSPACE
+    assert lib.m16_label_workspace_bytes(8, 8, 8) == nb
+    for conn in (0, 4, 8, 18):
+        assert lib.m16_label(fake, 8, 8, 8, conn, fake, ctypes.byref(n), fake, nb, None) == N.M16_ERR_BAD_ARG
+
+
+def test_dice_largest_validates_before_touching_the_gpu(lib):
+    from miccai2016_gb300 import _native as N
+    fake = ctypes.c_void_p(256)
+    d = ctypes.c_double(0.0)
+    nb = lib.m16_dice_largest_workspace_bytes(8, 8, 8)
+    assert nb > lib.m16_label_workspace_bytes(8, 8, 8) and lib.m16_dice_largest_workspace_bytes(8, 0, 8) == 0
+    assert lib.m16_dice_largest(fake, fake, 0, 8, 8, 0.5, ctypes.byref(d), None, None, fake, nb,
+                                None) == N.M16_ERR_BAD_SHAPE
+    assert lib.m16_dice_largest(None, fake, 8, 8, 8, 0.5, ctypes.byref(d), None, None, fake, nb,
+                                None) == N.M16_ERR_BAD_ARG
+    assert lib.m16_dice_largest(fake, fake, 8, 8, 8, 0.5, None, None, None, fake, nb, None) == N.M16_ERR_BAD_ARG
+    assert lib.m16_dice_largest(fake, fake, 8, 8, 8, 0.5, ctypes.byref(d), None, None, fake, nb - 1,
+                                None) == N.M16_ERR_WORKSPACE
 
 
 def test_host_tree_helpers(lib):

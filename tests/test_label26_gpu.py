@@ -73,3 +73,54 @@ def test_adjuster_with_gpu_labels_and_tree_matches_the_reference_logic():
         k1 = A.clean_ridge(ridge, c1, d1, (1.0, 1.0, 1.0))
         k2 = obj._do_clean_ridge(ridge, c2, d2)
     assert np.array_equal(k1, k2)
+
+
+@pytest.mark.parametrize("shape", [(40, 33, 50), (1, 64, 64), (7, 1, 300), (1, 1, 1)])
+@pytest.mark.parametrize("density", [0.0, 0.2, 0.5, 1.0])
+def test_six_connected_labels_equal_scipys_default(shape, density):
+    from miccai2016_gb300.labeling import label
+    rng = np.random.RandomState(int(density * 100) + sum(shape) + 6)
+    mask = rng.uniform(size=shape) < density
+    lab, n = label(mask, connectivity=6)
+    ref, rn = scipy.ndimage.label(mask)
+    assert n == rn and np.array_equal(lab, ref)
+
+
+def _blobs(rng, shape, k):
+    seg = np.zeros(shape, np.float32)
+    for _ in range(k):
+        c = rng.randint(0, shape, 3)
+        r = rng.randint(1, 5, 3)
+        sl = tuple(slice(max(0, c[a] - r[a]), c[a] + r[a]) for a in range(3))
+        seg[sl] = rng.uniform(0.5, 1.0)
+    return seg + rng.uniform(0, 0.49, shape).astype(np.float32)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_dice_of_the_largest_component_equals_the_host(seed):
+    from miccai2016_gb300 import phantom as P
+    from miccai2016_gb300.labeling import dice_largest
+    rng = np.random.RandomState(seed)
+    shape = tuple(rng.randint(8, 48, 3))
+    seg = _blobs(rng, shape, rng.randint(1, 12))
+    truth = _blobs(rng, shape, 3) >= 0.5
+    if seed == 4:
+        seg[3, 3, 3] = np.nan               # NaN is background, as numpy's comparison
+    assert dice_largest(seg, truth) == P.dice_largest(seg, truth)
+
+
+def test_dice_largest_ties_empty_and_full():
+    from miccai2016_gb300 import phantom as P
+    from miccai2016_gb300.labeling import dice_largest
+    shape = (10, 12, 14)
+    seg = np.zeros(shape, np.float32)
+    seg[1:3, 1:3, 1:3] = 1                  # two components of equal size: the first label wins
+    seg[6:8, 6:8, 6:8] = 1
+    truth = np.zeros(shape, bool)
+    truth[6:8, 6:8, 6:8] = True
+    assert dice_largest(seg, truth) == P.dice_largest(seg, truth) == 0.0
+    truth[1:3, 1:3, 1:2] = True
+    assert dice_largest(seg, truth) == P.dice_largest(seg, truth)
+    assert dice_largest(np.zeros(shape, np.float32), truth) == 0.0
+    full = np.ones(shape, np.float32)
+    assert dice_largest(full, truth) == P.dice_largest(full, truth)
