@@ -249,6 +249,8 @@ typedef struct m16_server_info {
     int64_t free_bytes;   /* workspace not held by requests */
     int64_t largest_free; /* largest request allocation that fits now */
     int64_t steps;        /* m16_server_step calls that ran iterations */
+    int64_t voxel_iterations; /* iterations run by the requests, times their voxels (useful work) */
+    double gpu_ms;        /* device time of the steps' kernels (CUDA events) */
 } m16_server_info;
 
 /* Workspace bytes a request of d0 x d1 x d2 voxels holds while resident. */

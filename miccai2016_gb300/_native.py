@@ -87,7 +87,8 @@ class ServeRequest(ctypes.Structure):
 class ServerInfo(ctypes.Structure):
     """m16_server_info (include/miccai2016_gb300.h)."""
     _fields_ = [("resident", _i32), ("draining", _i32), ("free_slots", _i32), ("reserved", _i32),
-                ("free_bytes", _i64), ("largest_free", _i64), ("steps", _i64)]
+                ("free_bytes", _i64), ("largest_free", _i64), ("steps", _i64), ("voxel_iterations", _i64),
+                ("gpu_ms", _f64)]
 
 
 def _declare(L):

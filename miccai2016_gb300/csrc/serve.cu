@@ -181,6 +181,7 @@ struct m16_server {
     m16_cut_params params;
     cudaStream_t stream = nullptr, copy = nullptr;
     cudaEvent_t step_done = nullptr;
+    cudaEvent_t t_start = nullptr, t_end = nullptr;   // timed events around each step's kernels
     char *ws = nullptr;
     size_t ws_bytes = 0;
     int max_slots = 0, max_work = 0;
@@ -199,6 +200,8 @@ struct m16_server {
     int seg_alpha = 0, n_items = 0;  // work items: [0, seg_alpha) alpha fields, [seg_alpha, n_items) (w, decay)
     int n_list = 0;                  // resident slots in list_h
     int64_t steps = 0;
+    int64_t voxel_iterations = 0;    // iterations that ran, times each request's voxels
+    double gpu_ms = 0.0;             // device time of the steps' kernels
     struct Done {
         int64_t tag;
         int iterations;
@@ -219,6 +222,8 @@ void release_host(m16_server *s)
     for (Slot &sl : s->slots)
         if (sl.ev) cudaEventDestroy(sl.ev);
     if (s->step_done) cudaEventDestroy(s->step_done);
+    if (s->t_start) cudaEventDestroy(s->t_start);
+    if (s->t_end) cudaEventDestroy(s->t_end);
     if (s->copy) cudaStreamDestroy(s->copy);
 }
 
@@ -313,6 +318,7 @@ extern "C" int m16_server_create(const m16_cut_params *params, int32_t max_slots
     for (int k = max_slots - 1; k >= 0; --k) s->free_slots.push_back(k);
     bool ok = cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking) == cudaSuccess &&
               cudaEventCreateWithFlags(&s->step_done, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreate(&s->t_start) == cudaSuccess && cudaEventCreate(&s->t_end) == cudaSuccess &&
               cudaMallocHost((void **)&s->stage, sizeof(Staging) * max_slots) == cudaSuccess &&
               cudaMallocHost((void **)&s->work_h, sizeof(int2) * (size_t)max_work_items) == cudaSuccess &&
               cudaMallocHost((void **)&s->list_h, sizeof(int) * max_slots) == cudaSuccess &&
@@ -464,6 +470,7 @@ extern "C" int m16_server_step(m16_server *s)
     float4 *dpart = (float4 *)s->ws;   // part_off counts float4 from the workspace start
     const dim3 block(kBX, kBY, 1);
     const int na = s->seg_alpha, ne = s->n_items - s->seg_alpha;
+    M16_CUDA_TRY(cudaEventRecord(s->t_start, st));
     for (int i = 0; i < s->params.update; ++i) {
         if (na > 0) bt1_flow_kernel<kAlphaArray><<<na, block, 0, st>>>(dwork, dvols, dgroups, dmask);
         if (ne > 0) bt1_flow_kernel<kAlphaFromGrad2><<<ne, block, 0, st>>>(dwork + na, dvols, dgroups, dmask);
@@ -476,15 +483,21 @@ extern "C" int m16_server_step(m16_server *s)
         }
     }
     M16_CUDA_TRY(cudaGetLastError());
+    M16_CUDA_TRY(cudaEventRecord(s->t_end, st));
     M16_CUDA_TRY(cudaEventRecord(s->step_done, st));
     M16_CUDA_TRY(cudaMemcpyAsync(s->ctrl_h, dctrl, sizeof(InstCtrl) * s->max_slots, cudaMemcpyDeviceToHost, st));
     M16_CUDA_TRY(cudaStreamSynchronize(st));
     s->steps += 1;
+    float step_ms = 0.f;
+    M16_CUDA_TRY(cudaEventElapsedTime(&step_ms, s->t_start, s->t_end));
+    s->gpu_ms += step_ms;
     for (int j = 0; j < s->n_list; ++j) {
         const int k = s->list_h[j];
         Slot &sl = s->slots[k];
         const InstCtrl &c = s->ctrl_h[k];
         sl.resid = c.resid;
+        // a request that stopped at this step's check ran that one iteration
+        s->voxel_iterations += sl.n * (c.stopped ? std::max(0, c.iterations - sl.iters_done) : s->params.update);
         if (c.stopped) {
             sl.iterations = c.iterations;
         } else {
@@ -529,6 +542,8 @@ extern "C" int m16_server_get_info(const m16_server *s, m16_server_info *info)
     info->free_bytes = (int64_t)s->arena.free_bytes();
     info->largest_free = (int64_t)s->arena.largest();
     info->steps = s->steps;
+    info->voxel_iterations = s->voxel_iterations;
+    info->gpu_ms = s->gpu_ms;
     return M16_OK;
 }
 

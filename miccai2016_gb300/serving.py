@@ -325,8 +325,11 @@ def served_vs_plain(n_requests=96, rate=50.0, pool=8, seed=0, max_resident=None,
     run_served(srv, payloads, warm)
     run_plain(payloads, warm)
     torch.cuda.synchronize()
+    info0 = srv.info()
     served = run_served(srv, payloads, reqs, max_resident=max_resident, keep=check)
     info = srv.info()
+    gpu_s = (info["gpu_ms"] - info0["gpu_ms"]) / 1000.0
+    vox_it = info["voxel_iterations"] - info0["voxel_iterations"]
     srv.close()
     torch.cuda.synchronize()
     plain = run_plain(payloads, reqs, keep=check)
@@ -345,7 +348,10 @@ def served_vs_plain(n_requests=96, rate=50.0, pool=8, seed=0, max_resident=None,
                 mean_voxels=float(np.mean(vox)), iterations={"median": float(np.median(its)), "max": int(max(its))},
                 max_u_diff_served_vs_plain=max(diffs) if diffs else None,
                 max_iteration_diff_served_vs_plain=max(itdiff) if itdiff else None,
-                server_steps=int(info["steps"]))
+                server_steps=int(info["steps"] - info0["steps"]),
+                server_gpu_busy=gpu_s / latency_summary(served)["span_s"],
+                server_voxel_iterations_per_gpu_s=vox_it / gpu_s if gpu_s > 0 else None,
+                server_gbs_at_84B_per_voxel_iteration=84.0 * vox_it / gpu_s / 1e9 if gpu_s > 0 else None)
 
 
 def _main(argv=None):
