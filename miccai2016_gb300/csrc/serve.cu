@@ -85,13 +85,20 @@ private:
     std::map<size_t, size_t> free_, used_;   // offset -> size
 };
 
-// z-chunk of a request's tiles: about four blocks per SM for the request
-// alone, at least two slices (the sweeps load two slices at a time)
+// z-chunk of a request's tiles: about M16_SERVE_BLOCKS_PER_SM blocks per SM
+// for the request alone, at least two slices (the sweeps load two slices at a
+// time)
+#ifndef M16_SERVE_BLOCKS_PER_SM
+#define M16_SERVE_BLOCKS_PER_SM 4
+#endif
+#ifndef M16_SERVE_MIN_ZC
+#define M16_SERVE_MIN_ZC 2
+#endif
 inline int serve_zc(int d0, int d1, int d2)
 {
     const int64_t cols = div_up(d2, kBX) * div_up(d1, kBY);
-    const int64_t zc = (int64_t)d0 * cols / (4 * kSMs);
-    return (int)std::max<int64_t>(2, std::min<int64_t>(32, zc));
+    const int64_t zc = (int64_t)d0 * cols / (M16_SERVE_BLOCKS_PER_SM * kSMs);
+    return (int)std::max<int64_t>(std::min<int64_t>(M16_SERVE_MIN_ZC, d0), std::min<int64_t>(32, zc));
 }
 
 // where a request's fields sit in its arena block
