@@ -227,7 +227,8 @@ def make_workload(n_requests, rate=50.0, pool=16, side_range=(64, 320), sigma_ra
 
 
 def _u_buffer(torch, shape):
-    return torch.empty(shape, dtype=torch.float32).pin_memory()
+    # allocated pinned (from the caching host allocator), not copied into pinned memory
+    return torch.empty(shape, dtype=torch.float32, pin_memory=True)
 
 
 def run_served(server, payloads, requests, max_resident=None, keep=None):
