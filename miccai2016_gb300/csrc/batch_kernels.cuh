@@ -113,10 +113,15 @@ inline int batch_zc(int d0, int d1, int d2, int ngroups_of_volume, int blocks_pe
 // One z-chunk for every volume of a launch: the launch covers the tiles of
 // all its groups, so the target number of blocks applies to their sum
 // (total_column_slices = sum over groups of d0 x the volume's 32 x 8 columns).
+#ifndef M16_BATCH_ZC_ROUND
+#define M16_BATCH_ZC_ROUND 1
+#endif
 inline int batch_zc_total(int64_t total_column_slices, int blocks_per_sm = M16_BATCH_BLOCKS_PER_SM)
 {
     int64_t zc = total_column_slices / ((int64_t)blocks_per_sm * kSMs);
-    return (int)std::max<int64_t>(1, std::min<int64_t>(32, zc));
+    zc = std::max<int64_t>(1, std::min<int64_t>(32, zc));
+    if (zc >= M16_BATCH_ZC_ROUND) zc = zc / M16_BATCH_ZC_ROUND * M16_BATCH_ZC_ROUND;
+    return (int)zc;
 }
 
 inline int64_t column_slices(int d0, int d1, int d2) { return (int64_t)d0 * div_up(d2, kBX) * div_up(d1, kBY); }
