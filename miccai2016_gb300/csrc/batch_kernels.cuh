@@ -114,7 +114,7 @@ inline int batch_zc(int d0, int d1, int d2, int ngroups_of_volume, int blocks_pe
 // all its groups, so the target number of blocks applies to their sum
 // (total_column_slices = sum over groups of d0 x the volume's 32 x 8 columns).
 #ifndef M16_BATCH_ZC_ROUND
-#define M16_BATCH_ZC_ROUND 1
+#define M16_BATCH_ZC_ROUND 4
 #endif
 inline int batch_zc_total(int64_t total_column_slices, int blocks_per_sm = M16_BATCH_BLOCKS_PER_SM)
 {
