@@ -407,6 +407,17 @@ __global__ void __launch_bounds__(kTile, M16_BATCH_MINB) bt_label_kernel(const i
 #ifndef M16_BATCH1_MINB
 #define M16_BATCH1_MINB 4
 #endif
+// z-slices whose loads the one-lane flow / label sweeps issue together:
+// measured on GB300 for one 256^3 instance of 1000 iterations, flow 1 /
+// label 4 takes 259 ms (alpha field: 257 ms), flow 2 / label 4 264 (285),
+// flow 1 / label 2 293 (291), flow 2 / label 2 297 (319); the single solve's
+// own sweeps take 232 ms
+#ifndef M16_BATCH1_FZB
+#define M16_BATCH1_FZB 1
+#endif
+#ifndef M16_BATCH1_UZB
+#define M16_BATCH1_UZB M16_MF_UZB
+#endif
 
 template <int ALPHA>
 __global__ void __launch_bounds__(kTile, M16_BATCH1_MINB) bt1_flow_kernel(const int2 *__restrict__ work,
@@ -437,7 +448,7 @@ __global__ void __launch_bounds__(kTile, M16_BATCH1_MINB) bt1_flow_kernel(const 
     f.q4 = V.q4;
     f.tmp = st + 4 * S;
     f.hp0 = st; f.hp1 = st + S; f.hp2 = st + 2 * S;
-    flow_column<false, ALPHA>(f, x, y, z0, z1);
+    flow_column<false, ALPHA, M16_BATCH1_FZB>(f, x, y, z0, z1);
 }
 
 template <bool CHECK>
@@ -465,7 +476,7 @@ __global__ void __launch_bounds__(kTile, M16_BATCH1_MINB) bt1_label_kernel(const
         l.hp0 = st; l.hp1 = st + S; l.hp2 = st + 2 * S;
         l.cs = V.cs; l.ct = V.ct; l.labels = nullptr;
         l.pt = st + 3 * S; l.tmp = st + 4 * S; l.u = st + 5 * S;
-        acc = label_column<false>(l, x, y, z0, z1);
+        acc = label_column<false, M16_BATCH1_UZB>(l, x, y, z0, z1);
     }
     if (CHECK) {
         const int tid = threadIdx.x + kBX * threadIdx.y;

@@ -108,19 +108,19 @@ __device__ __forceinline__ float label_point(float rcc, float rs0, float rs1, fl
 
 // P: p = H^-1 hp + H^T (steps grad tmp), projected onto |p| <= alpha, hp = H p
 // (update_qp.cl:150-232) for voxels (z0..z1, y, x).
-template <bool POINTWISE, int ALPHA>
+template <bool POINTWISE, int ALPHA, int kFZB = kMfZB>
 __device__ __forceinline__ void flow_column(const FlowView &a, int x, int y, int z0, int z1)
 {
     const int64_t s0 = (int64_t)a.d1 * a.d2;
     int64_t i = ((int64_t)z0 * a.d1 + y) * a.d2 + x;
     const bool yin = y < a.d1 - 1, xin = x < a.d2 - 1;
     float t = __ldg(a.tmp + i);
-    for (int zb = z0; zb < z1; zb += kMfZB, i += kMfZB * s0) {
-        float tz[kMfZB], ty[kMfZB], tx[kMfZB], al[kMfZB], h0[kMfZB], h1[kMfZB], h2[kMfZB];
-        float4 q[kMfZB];
-        float se0[kMfZB], se1[kMfZB], se2[kMfZB];
+    for (int zb = z0; zb < z1; zb += kFZB, i += kFZB * s0) {
+        float tz[kFZB], ty[kFZB], tx[kFZB], al[kFZB], h0[kFZB], h1[kFZB], h2[kFZB];
+        float4 q[kFZB];
+        float se0[kFZB], se1[kFZB], se2[kFZB];
 #pragma unroll
-        for (int k = 0; k < kMfZB; ++k) {
+        for (int k = 0; k < kFZB; ++k) {
             if (zb + k < z1) {
                 const int64_t j = i + k * s0;
                 tz[k] = (zb + k < a.d0 - 1) ? __ldg(a.tmp + j + s0) : 0.f;
@@ -141,7 +141,7 @@ __device__ __forceinline__ void flow_column(const FlowView &a, int x, int y, int
             }
         }
 #pragma unroll
-        for (int k = 0; k < kMfZB; ++k) {
+        for (int k = 0; k < kFZB; ++k) {
             if (zb + k < z1) {
                 const int64_t j = i + k * s0;
                 const float tc = k == 0 ? t : tz[k - 1];
@@ -159,7 +159,7 @@ __device__ __forceinline__ void flow_column(const FlowView &a, int x, int y, int
                 a.hp2[j] = h.z;
             }
         }
-        t = tz[kMfZB - 1];
+        t = tz[kFZB - 1];
     }
 }
 
