@@ -128,3 +128,31 @@ def test_admission_waits_for_memory_and_reuses_it():
     u, it = _plain(pls[1], 0.2, 3.0)
     assert [t for t, _, _ in done][-1] == 2
     assert np.max(np.abs(us[2].numpy() - u)) <= U_TOL
+
+
+def test_telemetry_counts_the_iterations_that_ran():
+    """m16_server_info.voxel_iterations is the sum over the finished requests
+    of voxels x iterations, and the steps' device time is positive."""
+    import torch
+    from miccai2016_gb300.serving import ATV_EIGS, CutServer
+    pls = _payloads()
+    srv = CutServer(num_iter=300, update=30, error_bound=1e-4, workspace_bytes=256 << 20, max_slots=16)
+    info0 = srv.info()
+    assert info0["voxel_iterations"] == 0 and info0["gpu_ms"] == 0.0
+    reqs = [(0, 0.05, 30.0), (1, 0.2, 10.0), (2, 0.01, 100.0), (0, 0.5, 3.0)]
+    done = {}
+    for tag, (pi, w, d) in enumerate(reqs):
+        u = torch.empty(pls[pi]["shape"], dtype=torch.float32, pin_memory=True)
+        assert srv.admit(tag, pls[pi], w, d, ATV_EIGS, u)
+    for _ in range(200):
+        srv.step()
+        for tag, it, res in srv.poll():
+            done[tag] = it
+        if len(done) == len(reqs):
+            break
+    assert len(done) == len(reqs)
+    info = srv.info()
+    want = sum(int(np.prod(pls[pi]["shape"])) * done[tag] for tag, (pi, _, _) in enumerate(reqs))
+    assert info["voxel_iterations"] == want
+    assert info["gpu_ms"] > 0.0
+    srv.close()
