@@ -777,10 +777,15 @@ def run_paths(args, cfg):
         e1.record(stream)
         torch.cuda.synchronize()
         k = solve(path, zc, timing=1)
-        return dict(ms_per_solve=e0.elapsed_time(e1) / args.steps, launches=s.launches,
-                    pair_launches=k.pair_launches, pair_zc=k.pair_zc, two_sweep_iterations=k.p_launches,
-                    pair_launch_ms=k.pair_ms / max(k.pair_launches, 1),
-                    flow_sweep_ms=k.p_ms / max(k.p_launches, 1), label_sweep_ms=k.u_ms / max(k.u_launches, 1))
+        r = dict(ms_per_solve=e0.elapsed_time(e1) / args.steps, launches=s.launches, iterations_timed=k.p_launches)
+        if path == N.PATH_PAIRS:
+            r.update(pair_launches=k.pair_launches, pair_zc=k.pair_zc,
+                     pair_launch_ms=k.pair_ms / max(k.pair_launches, 1))
+        if path == N.PATH_FUSED:
+            r.update(fused_launch_ms=k.p_ms / max(k.p_launches, 1))
+        elif k.u_launches > 0:
+            r.update(flow_sweep_ms=k.p_ms / max(k.p_launches, 1), label_sweep_ms=k.u_ms / max(k.u_launches, 1))
+        return r
 
     wanted = set(args.paths.split(","))
     out = {}
