@@ -777,7 +777,8 @@ def run_paths(args, cfg):
         e1.record(stream)
         torch.cuda.synchronize()
         k = solve(path, zc, timing=1)
-        r = dict(ms_per_solve=e0.elapsed_time(e1) / args.steps, launches=s.launches, iterations_timed=k.p_launches)
+        r = dict(ms_per_solve=e0.elapsed_time(e1) / args.steps, launches=s.launches,
+                 iterations_not_in_pairs=k.p_launches)
         if path == N.PATH_PAIRS:
             r.update(pair_launches=k.pair_launches, pair_zc=k.pair_zc,
                      pair_launch_ms=k.pair_ms / max(k.pair_launches, 1))
