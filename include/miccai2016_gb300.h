@@ -493,6 +493,18 @@ size_t m16_label_workspace_bytes(int32_t d0, int32_t d1, int32_t d2);
 int m16_label(const uint8_t *mask, int32_t d0, int32_t d1, int32_t d2, int32_t connectivity, int32_t *labels,
               int32_t *n_labels, void *workspace, size_t workspace_bytes, void *stream);
 
+/* Workspace bytes of m16_hysteresis (0 for invalid sizes). */
+size_t m16_hysteresis_workspace_bytes(int32_t d0, int32_t d1, int32_t d2);
+
+/*
+ * The hysteresis of the sign adjustment (ridge_detection.py:80-131): out = the
+ * voxels of the 26-connected components of (cand | sure) that hold a sure
+ * voxel -- the union of the reference's flood fills from every sure voxel.
+ * cand, sure, out: uint8 (device), nonzero = set.  Synchronizes `stream`.
+ */
+int m16_hysteresis(const uint8_t *cand, const uint8_t *sure, int32_t d0, int32_t d1, int32_t d2, uint8_t *out,
+                   void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- Dice of the largest connected component ---------------------------------------- */
 
 /* Workspace bytes of m16_dice_largest (0 for invalid sizes). */

@@ -135,6 +135,10 @@ def _declare(L):
     L.m16_label_workspace_bytes.argtypes = [_i32, _i32, _i32]
     L.m16_label.restype = ctypes.c_int
     L.m16_label.argtypes = [_vp, _i32, _i32, _i32, _i32, _vp, ctypes.POINTER(_i32), _vp, _sz, _vp]
+    L.m16_hysteresis_workspace_bytes.restype = _sz
+    L.m16_hysteresis_workspace_bytes.argtypes = [_i32, _i32, _i32]
+    L.m16_hysteresis.restype = ctypes.c_int
+    L.m16_hysteresis.argtypes = [_vp, _vp, _i32, _i32, _i32, _vp, _vp, _sz, _vp]
     L.m16_dice_largest_workspace_bytes.restype = _sz
     L.m16_dice_largest_workspace_bytes.argtypes = [_i32, _i32, _i32]
     L.m16_dice_largest.restype = ctypes.c_int

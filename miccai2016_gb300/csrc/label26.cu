@@ -263,6 +263,32 @@ __global__ void dl_intersect_kernel(const int32_t *__restrict__ labels, const ui
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(inter, (unsigned long long)c);
 }
 
+// ---- hysteresis: the candidate components that hold a sure voxel -------------
+
+__global__ void hy_union_mask_kernel(const uint8_t *__restrict__ cand, const uint8_t *__restrict__ sure, int64_t n,
+                                     uint8_t *__restrict__ both)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        both[i] = (cand[i] | sure[i]) ? 1 : 0;
+}
+
+// flag[label] = 1 for every label holding a sure voxel
+__global__ void hy_flag_kernel(const int32_t *__restrict__ labels, const uint8_t *__restrict__ sure, int64_t n,
+                               uint8_t *__restrict__ flag)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (sure[i]) flag[labels[i]] = 1;   // every writer stores 1: no atomics needed
+}
+
+__global__ void hy_select_kernel(const int32_t *__restrict__ labels, const uint8_t *__restrict__ flag, int64_t n,
+                                 uint8_t *__restrict__ out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t l = labels[i];
+        out[i] = l > 0 && flag[l] ? 1 : 0;
+    }
+}
+
 struct DlLayout {
     LbLayout lb;
     size_t mask, labels, sizes, ctrl, total;
@@ -373,4 +399,38 @@ extern "C" int m16_dice_largest(const float *seg, const uint8_t *truth, int32_t 
     const double den = (double)size + (double)h[0];
     *dice = size == 0 || den == 0.0 ? 0.0 : 2.0 * (double)h[2] / den;
     return M16_OK;
+}
+
+// The hysteresis of the sign adjustment (ridge_detection.py:80-131): the
+// voxels of the 26-connected components of (cand | sure) that hold a sure
+// voxel.  The workspace is m16_dice_largest's (mask, labels, per-label flags).
+extern "C" size_t m16_hysteresis_workspace_bytes(int32_t d0, int32_t d1, int32_t d2)
+{
+    return m16_dice_largest_workspace_bytes(d0, d1, d2);
+}
+
+extern "C" int m16_hysteresis(const uint8_t *cand, const uint8_t *sure, int32_t d0, int32_t d1, int32_t d2,
+                              uint8_t *out, void *workspace, size_t workspace_bytes, void *stream)
+{
+    if (!label_shape_ok(d0, d1, d2)) return M16_ERR_BAD_SHAPE;
+    if (!cand || !sure || !out) return M16_ERR_BAD_ARG;
+    const int64_t n = (int64_t)d0 * d1 * d2;
+    const DlLayout D = dl_layout(n);
+    if (!workspace || workspace_bytes < D.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *ws = (char *)workspace;
+    uint8_t *both = (uint8_t *)(ws + D.mask);
+    int32_t *labels = (int32_t *)(ws + D.labels);
+    uint8_t *flag = (uint8_t *)(ws + D.sizes);   // n + 1 bytes of the (n + 1) * 4 size area
+    hy_union_mask_kernel<<<lb_blocks(n), 256, 0, st>>>(cand, sure, n, both);
+    const int r = label_launch(both, d0, d1, d2, 26, labels, ws, D.lb, st);
+    if (r != M16_OK) return r;
+    M16_CUDA_TRY(cudaMemsetAsync(flag, 0, (size_t)(n + 1), st));
+    hy_flag_kernel<<<lb_blocks(n), 256, 0, st>>>(labels, sure, n, flag);
+    hy_select_kernel<<<lb_blocks(n), 256, 0, st>>>(labels, flag, n, out);
+    M16_CUDA_TRY(cudaGetLastError());
+    unsigned long long h = 0;
+    M16_CUDA_TRY(cudaMemcpyAsync(&h, ws + D.lb.ctrl, 8, cudaMemcpyDeviceToHost, st));
+    M16_CUDA_TRY(cudaStreamSynchronize(st));
+    return h != 0 ? M16_ERR_TIMEOUT : M16_OK;
 }

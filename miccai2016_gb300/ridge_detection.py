@@ -64,12 +64,25 @@ def hysteresis_threshold(cand, sure, labeler="gpu"):
     labels)."""
     from .labeling import label26
     assert cand.shape == sure.shape
-    both = np.logical_or(cand, sure)
-    labels, n = label26(both, where=labeler)
-    keep = np.zeros(n + 1, bool)
-    keep[np.unique(labels[np.asarray(sure, bool)])] = True
-    keep[0] = False
-    result = keep[labels]
+    if labeler == "gpu":
+        # labels, flags and the selection on the device (m16_hysteresis)
+        torch = N.torch_mod()
+        L = N.lib()
+        d0, d1, d2 = (int(v) for v in cand.shape)
+        dc = torch.from_numpy(np.ascontiguousarray(np.asarray(cand) != 0, dtype=np.uint8)).to(N.device())
+        dsu = torch.from_numpy(np.ascontiguousarray(np.asarray(sure) != 0, dtype=np.uint8)).to(N.device())
+        out = torch.empty((d0, d1, d2), dtype=torch.uint8, device=N.device())
+        ws = N.workspace(L.m16_hysteresis_workspace_bytes(d0, d1, d2))
+        N.check("m16_hysteresis", L.m16_hysteresis(N.ptr(dc), N.ptr(dsu), d0, d1, d2, N.ptr(out), N.ptr(ws),
+                                                   ws.numel(), N.stream_ptr()))
+        result = out.cpu().numpy().view(bool)
+    else:
+        both = np.logical_or(cand, sure)
+        labels, n = label26(both, where=labeler)
+        keep = np.zeros(n + 1, bool)
+        keep[np.unique(labels[np.asarray(sure, bool)])] = True
+        keep[0] = False
+        result = keep[labels]
     sure[...] = result
     cand[result] = False
     return sure

@@ -191,6 +191,16 @@ def test_label26_validates_before_touching_the_gpu(lib):
         assert lib.m16_label(fake, 8, 8, 8, conn, fake, ctypes.byref(n), fake, nb, None) == N.M16_ERR_BAD_ARG
 
 
+def test_hysteresis_validates_before_touching_the_gpu(lib):
+    from miccai2016_gb300 import _native as N
+    fake = ctypes.c_void_p(256)
+    nb = lib.m16_hysteresis_workspace_bytes(8, 8, 8)
+    assert nb == lib.m16_dice_largest_workspace_bytes(8, 8, 8) and lib.m16_hysteresis_workspace_bytes(0, 8, 8) == 0
+    assert lib.m16_hysteresis(fake, fake, 8, 0, 8, fake, fake, nb, None) == N.M16_ERR_BAD_SHAPE
+    assert lib.m16_hysteresis(fake, None, 8, 8, 8, fake, fake, nb, None) == N.M16_ERR_BAD_ARG
+    assert lib.m16_hysteresis(fake, fake, 8, 8, 8, fake, fake, nb - 1, None) == N.M16_ERR_WORKSPACE
+
+
 def test_dice_largest_validates_before_touching_the_gpu(lib):
     from miccai2016_gb300 import _native as N
     fake = ctypes.c_void_p(256)
