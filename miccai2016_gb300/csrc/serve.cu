@@ -11,6 +11,12 @@
 // the first), reads the stop mask, retires requests at the bound or at
 // num_iter, and starts their u downloads on the copy stream; poll() hands out
 // requests whose download has finished and returns their memory.
+//
+// Steps are pipelined by one: a step call enqueues the next step first and
+// only then waits for the previous step's stop mask, so the device runs while
+// the host retires, admits and polls.  A request that stopped in step k is
+// still listed (masked, no work) in step k + 1; its slot and memory are
+// reused only after the last step that lists it has been processed.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <float.h>
@@ -157,6 +163,8 @@ enum SlotState { kFree = 0, kResident = 1, kDraining = 2 };
 
 struct Slot {
     int state = kFree;
+    int iters_planned = 0;   // iterations of the steps enqueued so far (before any stop is known)
+    int64_t last_listed = -1;   // the last step whose work list holds the slot
     int64_t tag = 0;
     size_t block = 0;        // arena offset (from the arena's base)
     size_t u_off = 0;        // workspace offset of u
@@ -187,8 +195,10 @@ using namespace m16;
 struct m16_server {
     m16_cut_params params;
     cudaStream_t stream = nullptr, copy = nullptr;
-    cudaEvent_t step_done = nullptr;
-    cudaEvent_t t_start = nullptr, t_end = nullptr;   // timed events around each step's kernels
+    // per step parity (steps k and k + 1 are in flight together): the end of
+    // the step's kernels, its stop-mask copy, and timed events around its kernels
+    cudaEvent_t step_end[2] = {nullptr, nullptr}, ctrl_ev[2] = {nullptr, nullptr};
+    cudaEvent_t t_start[2] = {nullptr, nullptr}, t_end[2] = {nullptr, nullptr};
     char *ws = nullptr;
     size_t ws_bytes = 0;
     int max_slots = 0, max_work = 0;
@@ -200,13 +210,17 @@ struct m16_server {
     bool dirty = true;
     // pinned host buffers
     Staging *stage = nullptr;        // max_slots
-    int2 *work_h = nullptr;          // max_work
-    int *list_h = nullptr;           // max_slots
+    int2 *work_h[2] = {nullptr, nullptr};   // max_work each, by rebuild parity
+    int *list_h[2] = {nullptr, nullptr};    // max_slots each, by rebuild parity
     unsigned *mask_h = nullptr;      // max_slots
-    InstCtrl *ctrl_h = nullptr;      // max_slots
+    InstCtrl *ctrl_h[2] = {nullptr, nullptr};   // max_slots each, by step parity
     int seg_alpha = 0, n_items = 0;  // work items: [0, seg_alpha) alpha fields, [seg_alpha, n_items) (w, decay)
-    int n_list = 0;                  // resident slots in list_h
-    int64_t steps = 0;
+    int n_list = 0;                  // slots in the current list
+    int64_t rebuilds = 0;
+    std::vector<int> list_cur;       // the current list (host copy)
+    std::vector<int> step_list[2];   // the list of each step in flight, by step parity
+    int64_t steps = 0;               // steps enqueued
+    int64_t processed = 0;           // steps whose stop masks have been read (all steps < processed)
     int64_t voxel_iterations = 0;    // iterations that ran, times each request's voxels
     double gpu_ms = 0.0;             // device time of the steps' kernels
     struct Done {
@@ -222,62 +236,82 @@ namespace {
 void release_host(m16_server *s)
 {
     if (s->stage) cudaFreeHost(s->stage);
-    if (s->work_h) cudaFreeHost(s->work_h);
-    if (s->list_h) cudaFreeHost(s->list_h);
+    for (int b = 0; b < 2; ++b) {
+        if (s->work_h[b]) cudaFreeHost(s->work_h[b]);
+        if (s->list_h[b]) cudaFreeHost(s->list_h[b]);
+        if (s->ctrl_h[b]) cudaFreeHost(s->ctrl_h[b]);
+        if (s->step_end[b]) cudaEventDestroy(s->step_end[b]);
+        if (s->ctrl_ev[b]) cudaEventDestroy(s->ctrl_ev[b]);
+        if (s->t_start[b]) cudaEventDestroy(s->t_start[b]);
+        if (s->t_end[b]) cudaEventDestroy(s->t_end[b]);
+    }
     if (s->mask_h) cudaFreeHost(s->mask_h);
-    if (s->ctrl_h) cudaFreeHost(s->ctrl_h);
     for (Slot &sl : s->slots)
         if (sl.ev) cudaEventDestroy(sl.ev);
-    if (s->step_done) cudaEventDestroy(s->step_done);
-    if (s->t_start) cudaEventDestroy(s->t_start);
-    if (s->t_end) cudaEventDestroy(s->t_end);
     if (s->copy) cudaStreamDestroy(s->copy);
 }
 
-// rebuild the work list and the check list over the resident slots
+// rebuild the work list and the check list over the resident slots that
+// still have iterations to run.  The host sources alternate by rebuild: the
+// copy from a buffer is ordered before the step enqueued after it, which has
+// been processed (its stop mask read) before the buffer's next rebuild.
 int rebuild(m16_server *s)
 {
+    const int rb = (int)(s->rebuilds & 1);
+    int2 *work = s->work_h[rb];
+    int *list = s->list_h[rb];
     int nw = 0, nl = 0;
+    s->list_cur.clear();
     for (int pass = 0; pass < 2; ++pass) {
         if (pass == 1) s->seg_alpha = nw;
         for (int k = 0; k < s->max_slots; ++k) {
             const Slot &sl = s->slots[k];
             if (sl.state != kResident || sl.alpha != (pass == 0)) continue;
+            if (sl.iters_planned >= s->params.num_iter) continue;   // its last step is enqueued
             if (nw + sl.tiles > s->max_work) return M16_ERR_TOO_LARGE;
-            for (int t = 0; t < sl.tiles; ++t) s->work_h[nw++] = make_int2(k, t);
-            s->list_h[nl++] = k;
+            for (int t = 0; t < sl.tiles; ++t) work[nw++] = make_int2(k, t);
+            list[nl++] = k;
+            s->list_cur.push_back(k);
         }
     }
     s->n_items = nw;
     s->n_list = nl;
     if (nw > 0)
-        M16_CUDA_TRY(cudaMemcpyAsync(s->ws + s->T.work, s->work_h, sizeof(int2) * nw, cudaMemcpyHostToDevice,
-                                     s->stream));
+        M16_CUDA_TRY(cudaMemcpyAsync(s->ws + s->T.work, work, sizeof(int2) * nw, cudaMemcpyHostToDevice, s->stream));
     if (nl > 0)
-        M16_CUDA_TRY(cudaMemcpyAsync(s->ws + s->T.list, s->list_h, sizeof(int) * nl, cudaMemcpyHostToDevice,
-                                     s->stream));
+        M16_CUDA_TRY(cudaMemcpyAsync(s->ws + s->T.list, list, sizeof(int) * nl, cudaMemcpyHostToDevice, s->stream));
+    s->rebuilds += 1;
     s->dirty = false;
     return M16_OK;
 }
 
 // the retired slot's u goes to the host on the copy stream, after the step
-int start_download(m16_server *s, int k)
+// (of parity b) in which it became final
+int start_download(m16_server *s, int k, int b)
 {
     Slot &sl = s->slots[k];
     sl.state = kDraining;
-    M16_CUDA_TRY(cudaStreamWaitEvent(s->copy, s->step_done, 0));
+    M16_CUDA_TRY(cudaStreamWaitEvent(s->copy, s->step_end[b], 0));
     M16_CUDA_TRY(cudaMemcpyAsync(sl.u_host, s->ws + sl.u_off, sl.n * 4, cudaMemcpyDeviceToHost, s->copy));
     M16_CUDA_TRY(cudaEventRecord(sl.ev, s->copy));
     s->dirty = true;
     return M16_OK;
 }
 
-// hand out downloaded slots and return their memory
+int process_step(m16_server *s, int64_t idx);
+
+// hand out downloaded slots and return their memory: once the download has
+// finished and every step that lists the slot has been processed.  Steps
+// whose stop masks have arrived are processed first (without waiting), so the
+// last requests come back without another step call.
 void collect(m16_server *s)
 {
+    while (s->processed < s->steps && cudaEventQuery(s->ctrl_ev[s->processed & 1]) == cudaSuccess)
+        if (process_step(s, s->processed) != M16_OK) break;
     for (int k = 0; k < s->max_slots; ++k) {
         Slot &sl = s->slots[k];
-        if (sl.state != kDraining || cudaEventQuery(sl.ev) != cudaSuccess) continue;
+        if (sl.state != kDraining || sl.last_listed >= s->processed) continue;
+        if (cudaEventQuery(sl.ev) != cudaSuccess) continue;
         s->arena.release(sl.block);
         sl.state = kFree;
         s->free_slots.push_back(k);
@@ -324,13 +358,15 @@ extern "C" int m16_server_create(const m16_cut_params *params, int32_t max_slots
     s->slots.resize(max_slots);
     for (int k = max_slots - 1; k >= 0; --k) s->free_slots.push_back(k);
     bool ok = cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaEventCreateWithFlags(&s->step_done, cudaEventDisableTiming) == cudaSuccess &&
-              cudaEventCreate(&s->t_start) == cudaSuccess && cudaEventCreate(&s->t_end) == cudaSuccess &&
               cudaMallocHost((void **)&s->stage, sizeof(Staging) * max_slots) == cudaSuccess &&
-              cudaMallocHost((void **)&s->work_h, sizeof(int2) * (size_t)max_work_items) == cudaSuccess &&
-              cudaMallocHost((void **)&s->list_h, sizeof(int) * max_slots) == cudaSuccess &&
-              cudaMallocHost((void **)&s->mask_h, sizeof(unsigned) * max_slots) == cudaSuccess &&
-              cudaMallocHost((void **)&s->ctrl_h, sizeof(InstCtrl) * max_slots) == cudaSuccess;
+              cudaMallocHost((void **)&s->mask_h, sizeof(unsigned) * max_slots) == cudaSuccess;
+    for (int b = 0; ok && b < 2; ++b)
+        ok = cudaEventCreateWithFlags(&s->step_end[b], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&s->ctrl_ev[b], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreate(&s->t_start[b]) == cudaSuccess && cudaEventCreate(&s->t_end[b]) == cudaSuccess &&
+             cudaMallocHost((void **)&s->work_h[b], sizeof(int2) * (size_t)max_work_items) == cudaSuccess &&
+             cudaMallocHost((void **)&s->list_h[b], sizeof(int) * max_slots) == cudaSuccess &&
+             cudaMallocHost((void **)&s->ctrl_h[b], sizeof(InstCtrl) * max_slots) == cudaSuccess;
     for (int k = 0; ok && k < max_slots; ++k)
         ok = cudaEventCreateWithFlags(&s->slots[k].ev, cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
@@ -449,6 +485,8 @@ extern "C" int m16_server_admit(m16_server *s, const m16_serve_request *req, int
     sl.tiles = R.tx * R.ty * R.tz;
     sl.alpha = req->alpha != nullptr;
     sl.iters_done = 0;
+    sl.iters_planned = 0;
+    sl.last_listed = -1;
     sl.iterations = 0;
     sl.resid = NAN;
     sl.u_host = req->u;
@@ -457,51 +495,22 @@ extern "C" int m16_server_admit(m16_server *s, const m16_serve_request *req, int
     return M16_OK;
 }
 
-extern "C" int m16_server_step(m16_server *s)
+namespace {
+
+// read the stop mask of step idx (enqueued, not yet processed) and retire the
+// requests that stopped in it or ran their last iteration in it
+int process_step(m16_server *s, int64_t idx)
 {
-    if (!s) return M16_ERR_BAD_ARG;
-    collect(s);
-    if (s->dirty) {
-        const int r = rebuild(s);
-        if (r != M16_OK) return r;
-    }
-    if (s->n_list == 0) return M16_OK;
-    cudaStream_t st = s->stream;
-    const VolDev *dvols = (const VolDev *)(s->ws + s->T.vols);
-    const GroupDev *dgroups = (const GroupDev *)(s->ws + s->T.groups);
-    const InstDev *dinsts = (const InstDev *)(s->ws + s->T.insts);
-    InstCtrl *dctrl = (InstCtrl *)(s->ws + s->T.ctrl);
-    unsigned *dmask = (unsigned *)(s->ws + s->T.gmask);
-    const int2 *dwork = (const int2 *)(s->ws + s->T.work);
-    const int *dlist = (const int *)(s->ws + s->T.list);
-    float4 *dpart = (float4 *)s->ws;   // part_off counts float4 from the workspace start
-    const dim3 block(kBX, kBY, 1);
-    const int na = s->seg_alpha, ne = s->n_items - s->seg_alpha;
-    M16_CUDA_TRY(cudaEventRecord(s->t_start, st));
-    for (int i = 0; i < s->params.update; ++i) {
-        if (na > 0) bt1_flow_kernel<kAlphaArray><<<na, block, 0, st>>>(dwork, dvols, dgroups, dmask);
-        if (ne > 0) bt1_flow_kernel<kAlphaFromGrad2><<<ne, block, 0, st>>>(dwork + na, dvols, dgroups, dmask);
-        if (i == 0) {
-            bt1_label_kernel<true><<<s->n_items, block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
-            bt_check_kernel<<<s->n_list, 256, 0, st>>>(dvols, dgroups, dinsts, dctrl, dmask, dpart,
-                                                       s->params.error_bound, s->params.update, dlist);
-        } else {
-            bt1_label_kernel<false><<<s->n_items, block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
-        }
-    }
-    M16_CUDA_TRY(cudaGetLastError());
-    M16_CUDA_TRY(cudaEventRecord(s->t_end, st));
-    M16_CUDA_TRY(cudaEventRecord(s->step_done, st));
-    M16_CUDA_TRY(cudaMemcpyAsync(s->ctrl_h, dctrl, sizeof(InstCtrl) * s->max_slots, cudaMemcpyDeviceToHost, st));
-    M16_CUDA_TRY(cudaStreamSynchronize(st));
-    s->steps += 1;
+    if (idx != s->processed) return M16_ERR_BAD_ARG;   // in order only
+    const int b = (int)(idx & 1);
+    M16_CUDA_TRY(cudaEventSynchronize(s->ctrl_ev[b]));
     float step_ms = 0.f;
-    M16_CUDA_TRY(cudaEventElapsedTime(&step_ms, s->t_start, s->t_end));
+    M16_CUDA_TRY(cudaEventElapsedTime(&step_ms, s->t_start[b], s->t_end[b]));
     s->gpu_ms += step_ms;
-    for (int j = 0; j < s->n_list; ++j) {
-        const int k = s->list_h[j];
+    for (int k : s->step_list[b]) {
         Slot &sl = s->slots[k];
-        const InstCtrl &c = s->ctrl_h[k];
+        if (sl.state != kResident) continue;   // retired after an earlier step: masked here
+        const InstCtrl &c = s->ctrl_h[b][k];
         sl.resid = c.resid;
         // a request that stopped at this step's check ran that one iteration
         s->voxel_iterations += sl.n * (c.stopped ? std::max(0, c.iterations - sl.iters_done) : s->params.update);
@@ -512,7 +521,69 @@ extern "C" int m16_server_step(m16_server *s)
             if (sl.iters_done < s->params.num_iter) continue;
             sl.iterations = s->params.num_iter;
         }
-        const int r = start_download(s, k);
+        const int r = start_download(s, k, b);
+        if (r != M16_OK) return r;
+    }
+    s->processed = idx + 1;
+    return M16_OK;
+}
+
+}  // namespace
+
+extern "C" int m16_server_step(m16_server *s)
+{
+    if (!s) return M16_ERR_BAD_ARG;
+    collect(s);
+    if (s->dirty) {
+        const int r = rebuild(s);
+        if (r != M16_OK) return r;
+    }
+    const bool enqueue = s->n_list > 0;
+    if (enqueue) {
+        cudaStream_t st = s->stream;
+        const int64_t c = s->steps;
+        const int b = (int)(c & 1);   // step c - 2 of this parity has been processed
+        const VolDev *dvols = (const VolDev *)(s->ws + s->T.vols);
+        const GroupDev *dgroups = (const GroupDev *)(s->ws + s->T.groups);
+        const InstDev *dinsts = (const InstDev *)(s->ws + s->T.insts);
+        InstCtrl *dctrl = (InstCtrl *)(s->ws + s->T.ctrl);
+        unsigned *dmask = (unsigned *)(s->ws + s->T.gmask);
+        const int2 *dwork = (const int2 *)(s->ws + s->T.work);
+        const int *dlist = (const int *)(s->ws + s->T.list);
+        float4 *dpart = (float4 *)s->ws;   // part_off counts float4 from the workspace start
+        const dim3 block(kBX, kBY, 1);
+        const int na = s->seg_alpha, ne = s->n_items - s->seg_alpha;
+        M16_CUDA_TRY(cudaEventRecord(s->t_start[b], st));
+        for (int i = 0; i < s->params.update; ++i) {
+            if (na > 0) bt1_flow_kernel<kAlphaArray><<<na, block, 0, st>>>(dwork, dvols, dgroups, dmask);
+            if (ne > 0) bt1_flow_kernel<kAlphaFromGrad2><<<ne, block, 0, st>>>(dwork + na, dvols, dgroups, dmask);
+            if (i == 0) {
+                bt1_label_kernel<true><<<s->n_items, block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
+                bt_check_kernel<<<s->n_list, 256, 0, st>>>(dvols, dgroups, dinsts, dctrl, dmask, dpart,
+                                                           s->params.error_bound, s->params.update, dlist);
+            } else {
+                bt1_label_kernel<false><<<s->n_items, block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
+            }
+        }
+        M16_CUDA_TRY(cudaGetLastError());
+        M16_CUDA_TRY(cudaEventRecord(s->t_end[b], st));
+        M16_CUDA_TRY(cudaEventRecord(s->step_end[b], st));
+        M16_CUDA_TRY(cudaMemcpyAsync(s->ctrl_h[b], dctrl, sizeof(InstCtrl) * s->max_slots, cudaMemcpyDeviceToHost,
+                                     st));
+        M16_CUDA_TRY(cudaEventRecord(s->ctrl_ev[b], st));
+        s->step_list[b] = s->list_cur;
+        for (int k : s->list_cur) {
+            Slot &sl = s->slots[k];
+            sl.iters_planned += s->params.update;
+            sl.last_listed = c;
+            if (sl.iters_planned >= s->params.num_iter) s->dirty = true;   // out of the next list
+        }
+        s->steps = c + 1;
+    }
+    // the steps before the one just enqueued (all of them when none was)
+    const int64_t upto = enqueue ? s->steps - 1 : s->steps;
+    while (s->processed < upto) {
+        const int r = process_step(s, s->processed);
         if (r != M16_OK) return r;
     }
     return M16_OK;
