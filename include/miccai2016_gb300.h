@@ -214,6 +214,31 @@ int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const m16_batch_
                     const m16_cut_params *params, int32_t *iterations, double *residuals, void *workspace,
                     size_t workspace_bytes, void *stream, m16_solve_stats *stats);
 
+/*
+ * The same batch as a sequence of steps.  m16_batch_begin prepares the batch
+ * on `stream` (descriptors, set-up kernels, the default tile shape, a work
+ * list over every group; nothing is synchronised) and returns a handle.
+ * m16_batch_iterate enqueues `count` iterations (not past num_iter), with a
+ * residual check on every iteration index that is a multiple of update, and
+ * does nothing else: no synchronisation, allocation or copy, so a caller may
+ * capture it into a CUDA graph.  A graph captured from a call that starts at
+ * a multiple of update and runs update iterations replays one check interval.
+ * Instances stop at their residual bound on the device (their lanes are
+ * masked).  m16_batch_end scatters every instance's u to its output, reports
+ * iterations (at the stop, else the iterations that ran) and the last
+ * residuals, and frees the handle; it synchronizes `stream`.  The three calls
+ * take the same stream (or the caller orders them).  The workspace
+ * (m16_batch_workspace_bytes) and the inputs must stay valid until the end.
+ * Graph replays are not bounded by num_iter: the caller replays at most the
+ * check intervals num_iter allows.
+ */
+typedef struct m16_batch m16_batch;
+int m16_batch_begin(const m16_batch_volume *vols, int32_t nvol, const m16_batch_instance *inst, int32_t ninst,
+                    const m16_cut_params *params, void *workspace, size_t workspace_bytes, void *stream,
+                    m16_batch **out);
+int m16_batch_iterate(m16_batch *b, int32_t count, void *stream);
+int m16_batch_end(m16_batch *b, int32_t *iterations, double *residuals, void *stream);
+
 /* ---- serving: continuous batching of max-flow requests ----------------------
  * No reference interface: the reference solves one CmfCutQAnisotropicGpu at a
  * time.  A server owns one caller workspace; requests (each its own volume)

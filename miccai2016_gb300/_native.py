@@ -164,6 +164,13 @@ def _declare(L):
     L.m16_batch_solve.restype = ctypes.c_int
     L.m16_batch_solve.argtypes = [ctypes.POINTER(BatchVolume), _i32, ctypes.POINTER(BatchInstance), _i32,
                                   ctypes.POINTER(CutParams), _vp, _vp, _vp, _sz, _vp, ctypes.POINTER(SolveStats)]
+    L.m16_batch_begin.restype = ctypes.c_int
+    L.m16_batch_begin.argtypes = [ctypes.POINTER(BatchVolume), _i32, ctypes.POINTER(BatchInstance), _i32,
+                                  ctypes.POINTER(CutParams), _vp, _sz, _vp, ctypes.POINTER(_vp)]
+    L.m16_batch_iterate.restype = ctypes.c_int
+    L.m16_batch_iterate.argtypes = [_vp, _i32, _vp]
+    L.m16_batch_end.restype = ctypes.c_int
+    L.m16_batch_end.argtypes = [_vp, _vp, _vp, _vp]
     L.m16_server_request_bytes.restype = _sz
     L.m16_server_request_bytes.argtypes = [_i32, _i32, _i32, _i32]
     L.m16_server_table_bytes.restype = _sz

@@ -98,6 +98,78 @@ class BatchedCut(object):
         self.last_blocks_per_sm = int(stats.blocks_per_sm)
         return us
 
+    def _describe(self, volumes, instances):
+        """ctypes descriptors of a batch, the u outputs and the buffers that
+        must stay alive while it runs."""
+        torch = N.torch_mod()
+        nv, ni = len(volumes), len(instances)
+        vd = (N.BatchVolume * nv)()
+        for k, v in enumerate(volumes):
+            d0, d1, d2 = v["shape"]
+            vd[k] = N.BatchVolume(d0, d1, d2, 0, N.ptr(v["img"]), N.ptr(v["quats"]), N.ptr(v["grad2"]),
+                                  N.ptr(v["cs"]), N.ptr(v["ct"]), (ctypes.c_double * 3)(*v["scaling"]))
+        us, keep = [], []
+        idesc = (N.BatchInstance * ni)()
+        for k, inst in enumerate(instances):
+            shape = volumes[inst["volume"]]["shape"]
+            u = torch.empty(shape, dtype=torch.float32, device=N.device())
+            us.append(u)
+            alpha = inst.get("alpha")
+            if alpha is not None:
+                alpha = N.to_device_f32(alpha, shape)
+                keep.append(alpha)
+            sq = np.sqrt(np.asarray(inst["eigs"], dtype=np.float64))
+            idesc[k] = N.BatchInstance(int(inst["volume"]), 0, float(inst.get("weighting", 0.0)),
+                                       float(inst.get("decay", 0.0)), N.ptr(alpha), (ctypes.c_double * 3)(*sq),
+                                       N.ptr(u))
+        return vd, idesc, us, keep
+
+    def begin(self, volumes, instances):
+        """The batch as capture-safe steps (m16_batch_begin): returns a
+        BatchSteps whose iterate(count) only enqueues kernels on the current
+        stream (so it may be captured into a CUDA graph) and whose end()
+        returns the u of every instance."""
+        return BatchSteps(self, volumes, instances)
+
+
+class BatchSteps(object):
+    """m16_batch_begin / m16_batch_iterate / m16_batch_end over one batch."""
+
+    def __init__(self, cut, volumes, instances):
+        L = N.lib()
+        self._L = L
+        self._vd, self._idesc, self._us, self._keep = cut._describe(volumes, instances)
+        self._volumes = volumes
+        p = cut.params
+        self._cp = N.CutParams(float(p.cc), float(p.steps), float(p.error_bound), int(p.num_iter), int(p.update),
+                               (ctypes.c_double * 3)(1.0, 1.0, 1.0))
+        nbytes = L.m16_batch_workspace_bytes(self._vd, len(volumes), self._idesc, len(instances))
+        if nbytes == 0:
+            raise ValueError("invalid batch description")
+        self._ws = N.workspace(nbytes)
+        self._n = len(instances)
+        h = ctypes.c_void_p()
+        N.check("m16_batch_begin", L.m16_batch_begin(self._vd, len(volumes), self._idesc, self._n,
+                                                     ctypes.byref(self._cp), N.ptr(self._ws), self._ws.numel(),
+                                                     N.stream_ptr(), ctypes.byref(h)))
+        self._h = h
+        self.iterations = None
+        self.residuals = None
+
+    def iterate(self, count):
+        N.check("m16_batch_iterate", self._L.m16_batch_iterate(self._h, int(count), N.stream_ptr()))
+
+    def end(self):
+        """u of every instance (CUDA tensors, instance order); sets
+        .iterations and .residuals."""
+        its = (ctypes.c_int32 * self._n)()
+        res = (ctypes.c_double * self._n)()
+        h, self._h = self._h, None
+        N.check("m16_batch_end", self._L.m16_batch_end(h, its, res, N.stream_ptr()))
+        self.iterations = np.array(its[:], np.int64)
+        self.residuals = np.array(res[:], np.float64)
+        return self._us
+
 
 def _main(argv=None):
     """Timing of one batch: python -m miccai2016_gb300.batched --side 128 --instances 64

@@ -177,34 +177,44 @@ bool batch_args_ok(const m16_batch_volume *vols, int nvol, const m16_batch_insta
     return true;
 }
 
-}  // namespace
-}  // namespace m16
+// The host copies of a batch's descriptors and the device addresses of its
+// tables, filled by batch_prepare (which also uploads the descriptors and runs
+// the per-volume and per-group set-up kernels on the stream).
+struct BatchRun {
+    Plan P;
+    BatchLayout L;
+    int ngroups = 0;
+    std::vector<VolDev> hv;
+    std::vector<GroupDev> hg;
+    std::vector<unsigned> hmask;
+    std::vector<InstDev> hi;
+    std::vector<InstCtrl> hctrl;
+    VolDev *dvols = nullptr;
+    GroupDev *dgroups = nullptr;
+    InstDev *dinsts = nullptr;
+    InstCtrl *dctrl = nullptr;
+    unsigned *dmask = nullptr;
+    int2 *dwork = nullptr;
+    float4 *dpart = nullptr;
+};
 
-using namespace m16;
-
-extern "C" size_t m16_batch_workspace_bytes(const m16_batch_volume *vols, int32_t nvol,
-                                            const m16_batch_instance *inst, int32_t ninst)
+int batch_prepare(const m16_batch_volume *vols, int nvol, const m16_batch_instance *inst, int ninst,
+                  const m16_cut_params *params, char *ws, cudaStream_t st, BatchRun &B, int &launches)
 {
-    if (!batch_args_ok(vols, nvol, inst, ninst)) return 0;
-    return batch_layout(vols, nvol, inst, ninst, make_plan(nvol, inst, ninst)).total;
-}
-
-extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const m16_batch_instance *inst,
-                               int32_t ninst, const m16_cut_params *params, int32_t *iterations, double *residuals,
-                               void *workspace, size_t workspace_bytes, void *stream, m16_solve_stats *stats)
-{
-    if (!params || params->update < 1 || params->num_iter < 0 || !(params->cc > 0.0)) return M16_ERR_BAD_ARG;
-    if (!batch_args_ok(vols, nvol, inst, ninst)) return M16_ERR_BAD_ARG;
-    if (stats && (stats->path < M16_PATH_DEFAULT || stats->path > M16_PATH_FUSED)) return M16_ERR_BAD_ARG;
-    const Plan P = make_plan(nvol, inst, ninst);
-    const BatchLayout L = batch_layout(vols, nvol, inst, ninst, P);
-    if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;
-    cudaStream_t st = (cudaStream_t)stream;
-    char *ws = (char *)workspace;
-    const int ngroups = (int)P.group_insts.size();
-
+    const Plan &P = B.P;
+    const BatchLayout &L = B.L;
+    const int ngroups = B.ngroups;
+    std::vector<VolDev> &hv = B.hv;
+    std::vector<GroupDev> &hg = B.hg;
+    std::vector<unsigned> &hmask = B.hmask;
+    std::vector<InstDev> &hi = B.hi;
+    std::vector<InstCtrl> &hctrl = B.hctrl;
+    hv.assign(nvol, VolDev());
+    hg.assign(ngroups, GroupDev());
+    hmask.assign(ngroups, 0u);
+    hi.assign(ninst, InstDev());
+    hctrl.assign(ninst, InstCtrl());
     // device descriptors
-    std::vector<VolDev> hv(nvol);
     for (int v = 0; v < nvol; ++v) {
         const m16_batch_volume &V = vols[v];
         VolDev &d = hv[v];
@@ -223,8 +233,6 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         d.grad2 = V.grad2; d.cs = V.cs; d.ct = V.ct;
         d.n = (int64_t)V.d0 * V.d1 * V.d2;
     }
-    std::vector<GroupDev> hg(ngroups);
-    std::vector<unsigned> hmask(ngroups, 0u);
     for (int g = 0; g < ngroups; ++g) {
         GroupDev &d = hg[g];
         const std::vector<int> &lanes = P.group_insts[g];
@@ -257,14 +265,12 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         const size_t esz = d.lanes == kLanes ? 16 : 4;
         d.slab = (int64_t)(align_up(hv[d.vol].n * esz, 256) / esz);
     }
-    std::vector<InstDev> hi(ninst);
     for (int i = 0; i < ninst; ++i) {
         hi[i].group = P.inst_group[i];
         hi[i].lane = P.inst_lane[i];
         hi[i].u_out = inst[i].u;
         hi[i].alpha = inst[i].alpha;
     }
-    std::vector<InstCtrl> hctrl(ninst);
     for (int i = 0; i < ninst; ++i) {
         hctrl[i].stopped = 0;
         hctrl[i].iterations = params->num_iter;
@@ -272,13 +278,13 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         hctrl[i].pad = 0;
         hctrl[i].resid = NAN;
     }
-    VolDev *dvols = (VolDev *)(ws + L.vols);
-    GroupDev *dgroups = (GroupDev *)(ws + L.groups);
-    InstDev *dinsts = (InstDev *)(ws + L.insts);
-    InstCtrl *dctrl = (InstCtrl *)(ws + L.ctrl);
-    unsigned *dmask = (unsigned *)(ws + L.gmask);
-    int2 *dwork = (int2 *)(ws + L.work);
-    float4 *dpart = (float4 *)(ws + L.partials);
+    VolDev *dvols = B.dvols = (VolDev *)(ws + L.vols);
+    GroupDev *dgroups = B.dgroups = (GroupDev *)(ws + L.groups);
+    InstDev *dinsts = B.dinsts = (InstDev *)(ws + L.insts);
+    InstCtrl *dctrl = B.dctrl = (InstCtrl *)(ws + L.ctrl);
+    unsigned *dmask = B.dmask = (unsigned *)(ws + L.gmask);
+    B.dwork = (int2 *)(ws + L.work);
+    B.dpart = (float4 *)(ws + L.partials);
     M16_CUDA_TRY(cudaMemcpyAsync(dvols, hv.data(), sizeof(VolDev) * nvol, cudaMemcpyHostToDevice, st));
     M16_CUDA_TRY(cudaMemcpyAsync(dgroups, hg.data(), sizeof(GroupDev) * ngroups, cudaMemcpyHostToDevice, st));
     M16_CUDA_TRY(cudaMemcpyAsync(dinsts, hi.data(), sizeof(InstDev) * ninst, cudaMemcpyHostToDevice, st));
@@ -286,7 +292,6 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     M16_CUDA_TRY(cudaMemcpyAsync(dmask, hmask.data(), sizeof(unsigned) * ngroups, cudaMemcpyHostToDevice, st));
 
     // per-volume set-up, then per-group state
-    int launches = 0;
     for (int v = 0; v < nvol; ++v) {
         const int blocks = (int)std::min<int64_t>(kMaxBlocks, div_up(hv[v].n, 256));
         float *mp = (float *)(ws + L.maxpart[v]);
@@ -309,6 +314,98 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         }
     }
     M16_CUDA_TRY(cudaGetLastError());
+
+    return M16_OK;
+}
+
+// one iteration's launches on stream s: the flow sweeps of the four
+// work-list segments, the label sweeps, and on check iterations the residual
+// check; e0..e2 (optional) bracket the flow and the label launches.  Returns
+// the number of launches.
+int launch_iteration(const BatchRun &B, const int *seg, int ninst, const m16_cut_params *params, cudaStream_t s,
+                     bool check, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2)
+{
+    const dim3 block(kBX, kBY, 1);
+    int n = 0;
+    if (e0) cudaEventRecord(e0, s);
+    const int n4 = seg[2], n1 = seg[4] - seg[2];
+    if (seg[1] > seg[0])
+        bt_flow_kernel<true><<<seg[1] - seg[0], block, 0, s>>>(B.dwork + seg[0], B.dvols, B.dgroups, B.dmask);
+    if (seg[2] > seg[1])
+        bt_flow_kernel<false><<<seg[2] - seg[1], block, 0, s>>>(B.dwork + seg[1], B.dvols, B.dgroups, B.dmask);
+    if (seg[3] > seg[2])
+        bt1_flow_kernel<kAlphaArray><<<seg[3] - seg[2], block, 0, s>>>(B.dwork + seg[2], B.dvols, B.dgroups,
+                                                                        B.dmask);
+    if (seg[4] > seg[3])
+        bt1_flow_kernel<kAlphaFromGrad2><<<seg[4] - seg[3], block, 0, s>>>(B.dwork + seg[3], B.dvols, B.dgroups,
+                                                                            B.dmask);
+    if (e1) cudaEventRecord(e1, s);
+    if (n4 > 0) {
+        if (check) bt_label_kernel<true><<<n4, block, 0, s>>>(B.dwork, B.dvols, B.dgroups, B.dmask, B.dpart);
+        else bt_label_kernel<false><<<n4, block, 0, s>>>(B.dwork, B.dvols, B.dgroups, B.dmask, B.dpart);
+    }
+    if (n1 > 0) {
+        if (check)
+            bt1_label_kernel<true><<<n1, block, 0, s>>>(B.dwork + seg[2], B.dvols, B.dgroups, B.dmask, B.dpart);
+        else
+            bt1_label_kernel<false><<<n1, block, 0, s>>>(B.dwork + seg[2], B.dvols, B.dgroups, B.dmask, B.dpart);
+    }
+    if (e2) cudaEventRecord(e2, s);
+    for (int k = 0; k < 4; ++k) n += seg[k + 1] > seg[k];
+    n += (n4 > 0) + (n1 > 0);
+    if (check) {
+        bt_check_kernel<<<ninst, 256, 0, s>>>(B.dvols, B.dgroups, B.dinsts, B.dctrl, B.dmask, B.dpart,
+                                              params->error_bound, params->update, nullptr);
+        ++n;
+    }
+    return n;
+}
+
+}  // namespace
+}  // namespace m16
+
+using namespace m16;
+
+extern "C" size_t m16_batch_workspace_bytes(const m16_batch_volume *vols, int32_t nvol,
+                                            const m16_batch_instance *inst, int32_t ninst)
+{
+    if (!batch_args_ok(vols, nvol, inst, ninst)) return 0;
+    return batch_layout(vols, nvol, inst, ninst, make_plan(nvol, inst, ninst)).total;
+}
+
+extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const m16_batch_instance *inst,
+                               int32_t ninst, const m16_cut_params *params, int32_t *iterations, double *residuals,
+                               void *workspace, size_t workspace_bytes, void *stream, m16_solve_stats *stats)
+{
+    if (!params || params->update < 1 || params->num_iter < 0 || !(params->cc > 0.0)) return M16_ERR_BAD_ARG;
+    if (!batch_args_ok(vols, nvol, inst, ninst)) return M16_ERR_BAD_ARG;
+    if (stats && (stats->path < M16_PATH_DEFAULT || stats->path > M16_PATH_FUSED)) return M16_ERR_BAD_ARG;
+    const Plan P = make_plan(nvol, inst, ninst);
+    const BatchLayout L = batch_layout(vols, nvol, inst, ninst, P);
+    if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *ws = (char *)workspace;
+    const int ngroups = (int)P.group_insts.size();
+
+    BatchRun B;
+    B.P = P;
+    B.L = L;
+    B.ngroups = ngroups;
+    int launches = 0;
+    {
+        const int r = batch_prepare(vols, nvol, inst, ninst, params, ws, st, B, launches);
+        if (r != M16_OK) return r;
+    }
+    std::vector<VolDev> &hv = B.hv;
+    std::vector<GroupDev> &hg = B.hg;
+    std::vector<unsigned> &hmask = B.hmask;
+    std::vector<InstCtrl> &hctrl = B.hctrl;
+    VolDev *dvols = B.dvols;
+    GroupDev *dgroups = B.dgroups;
+    InstDev *dinsts = B.dinsts;
+    InstCtrl *dctrl = B.dctrl;
+    unsigned *dmask = B.dmask;
+    int2 *dwork = B.dwork;
 
     // the work list: per group and tile, groups with an active lane only, in
     // four segments (the sweeps are compiled per group kind): four-lane with
@@ -404,42 +501,13 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     int it = 0;
     int n_groups_active = ngroups;
     int listed = ngroups;   // groups in the current work list
-    const dim3 block(kBX, kBY, 1);
 
     // one iteration's launches on stream `s`: the flow sweeps of the four
     // work-list segments, the label sweeps, and on check iterations the
     // residual check; returns the number of launches
     auto enqueue_iteration = [&](cudaStream_t s, bool check, bool time_it) -> int {
-        int n = 0;
-        if (time_it) cudaEventRecord(e0, s);
-        const int n4 = seg[2], n1 = seg[4] - seg[2];
-        if (seg[1] > seg[0])
-            bt_flow_kernel<true><<<seg[1] - seg[0], block, 0, s>>>(dwork + seg[0], dvols, dgroups, dmask);
-        if (seg[2] > seg[1])
-            bt_flow_kernel<false><<<seg[2] - seg[1], block, 0, s>>>(dwork + seg[1], dvols, dgroups, dmask);
-        if (seg[3] > seg[2])
-            bt1_flow_kernel<kAlphaArray><<<seg[3] - seg[2], block, 0, s>>>(dwork + seg[2], dvols, dgroups, dmask);
-        if (seg[4] > seg[3])
-            bt1_flow_kernel<kAlphaFromGrad2><<<seg[4] - seg[3], block, 0, s>>>(dwork + seg[3], dvols, dgroups,
-                                                                            dmask);
-        if (time_it) cudaEventRecord(e1, s);
-        if (n4 > 0) {
-            if (check) bt_label_kernel<true><<<n4, block, 0, s>>>(dwork, dvols, dgroups, dmask, dpart);
-            else bt_label_kernel<false><<<n4, block, 0, s>>>(dwork, dvols, dgroups, dmask, dpart);
-        }
-        if (n1 > 0) {
-            if (check) bt1_label_kernel<true><<<n1, block, 0, s>>>(dwork + seg[2], dvols, dgroups, dmask, dpart);
-            else bt1_label_kernel<false><<<n1, block, 0, s>>>(dwork + seg[2], dvols, dgroups, dmask, dpart);
-        }
-        if (time_it) cudaEventRecord(e2, s);
-        for (int k = 0; k < 4; ++k) n += seg[k + 1] > seg[k];
-        n += (n4 > 0) + (n1 > 0);
-        if (check) {
-            bt_check_kernel<<<ninst, 256, 0, s>>>(dvols, dgroups, dinsts, dctrl, dmask, dpart, params->error_bound,
-                                                  update, nullptr);
-            ++n;
-        }
-        return n;
+        return launch_iteration(B, seg, ninst, params, s, check, time_it ? e0 : nullptr, time_it ? e1 : nullptr,
+                                time_it ? e2 : nullptr);
     };
 
     // Full chunks (chunk iterations starting at a multiple of `update`, so
@@ -593,4 +661,147 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
         stats->u_ms = u_ms;
     }
     return M16_OK;
+}
+
+// ---- the batch as a sequence of capture-safe steps ------------------------------
+//
+// m16_batch_begin prepares a batch on the stream (descriptors, set-up
+// kernels, the default tile shape and a work list over every group) and
+// returns a handle; m16_batch_iterate enqueues iterations and does nothing
+// else -- no synchronisation, no allocation, no copies -- so a caller may
+// capture it into a CUDA graph of its own; m16_batch_end scatters every
+// instance's u to its output, reads the iteration counts and residuals and
+// frees the handle.  Instances stop on the device at their residual bound
+// (their lanes are masked); the work list is not shrunk between steps.
+
+struct m16_batch {
+    BatchRun B;
+    std::vector<m16_batch_instance> inst;
+    std::vector<int64_t> inst_n;    // voxels of each instance's volume
+    m16_cut_params params;
+    std::vector<int2> work;
+    int seg[5] = {0, 0, 0, 0, 0};
+    int ninst = 0;
+    int iterations_run = 0;          // iterations enqueued by m16_batch_iterate
+};
+
+extern "C" int m16_batch_begin(const m16_batch_volume *vols, int32_t nvol, const m16_batch_instance *inst,
+                               int32_t ninst, const m16_cut_params *params, void *workspace, size_t workspace_bytes,
+                               void *stream, m16_batch **out)
+{
+    if (!out) return M16_ERR_BAD_ARG;
+    *out = nullptr;
+    if (!params || params->update < 1 || params->num_iter < 0 || !(params->cc > 0.0)) return M16_ERR_BAD_ARG;
+    if (!batch_args_ok(vols, nvol, inst, ninst)) return M16_ERR_BAD_ARG;
+    m16_batch *b = new m16_batch();
+    b->B.P = make_plan(nvol, inst, ninst);
+    b->B.L = batch_layout(vols, nvol, inst, ninst, b->B.P);
+    if (!workspace || workspace_bytes < b->B.L.total || ((uintptr_t)workspace & 255)) {
+        delete b;
+        return M16_ERR_WORKSPACE;
+    }
+    b->B.ngroups = (int)b->B.P.group_insts.size();
+    b->params = *params;
+    b->ninst = ninst;
+    b->inst.assign(inst, inst + ninst);
+    cudaStream_t st = (cudaStream_t)stream;
+    char *ws = (char *)workspace;
+    int launches = 0;
+    const int r = batch_prepare(vols, nvol, inst, ninst, params, ws, st, b->B, launches);
+    if (r != M16_OK) {
+        delete b;
+        return r;
+    }
+    BatchRun &B = b->B;
+    for (int i = 0; i < ninst; ++i) b->inst_n.push_back(B.hv[inst[i].volume].n);
+    // the default tile shape (one z-chunk over the whole launch's work)
+    int64_t total_cs = 0;
+    for (int v = 0; v < nvol; ++v)
+        total_cs += column_slices(B.hv[v].d0, B.hv[v].d1, B.hv[v].d2) * B.P.ngroups_of_vol[v];
+    const int zc = batch_zc_total(total_cs, M16_BATCH_BLOCKS_PER_SM);
+    for (int v = 0; v < nvol; ++v) {
+        VolDev &d = B.hv[v];
+        d.zc = zc;
+        d.tz = (int)div_up(d.d0, d.zc);
+        // only zc..tz: the set-up kernels write the denominator on the device
+        if (cudaMemcpyAsync((char *)(B.dvols + v) + offsetof(VolDev, zc), &d.zc, 4 * sizeof(int),
+                            cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            delete b;
+            return M16_ERR_CUDA;
+        }
+    }
+    int64_t off = 0;
+    for (int g = 0; g < B.ngroups; ++g) {
+        const VolDev &V = B.hv[B.hg[g].vol];
+        B.hg[g].part_off = off;
+        B.hg[g].nparts = V.tx * V.ty * V.tz;
+        off += B.hg[g].nparts;
+    }
+    // work list: groups with an active lane, four segments by group kind
+    auto kind_of = [&](int g) { return (B.hg[g].lanes == kLanes ? 0 : 2) + (B.hg[g].has_alpha ? 0 : 1); };
+    for (int k = 0; k < 4; ++k) {
+        b->seg[k] = (int)b->work.size();
+        for (int g = 0; g < B.ngroups; ++g) {
+            if (B.hmask[g] == kAllLanes || kind_of(g) != k) continue;
+            const VolDev &V = B.hv[B.hg[g].vol];
+            const int ntiles = V.tx * V.ty * V.tz;
+            for (int t = 0; t < ntiles; ++t) b->work.push_back(make_int2(g, t));
+        }
+    }
+    b->seg[4] = (int)b->work.size();
+    // the handle owns the host sources until the copies have run
+    if (cudaMemcpyAsync(B.dgroups, B.hg.data(), sizeof(GroupDev) * B.ngroups, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        (!b->work.empty() && cudaMemcpyAsync(B.dwork, b->work.data(), sizeof(int2) * b->work.size(),
+                                             cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+        cudaGetLastError() != cudaSuccess) {
+        cudaStreamSynchronize(st);
+        delete b;
+        return M16_ERR_CUDA;
+    }
+    *out = b;
+    return M16_OK;
+}
+
+extern "C" int m16_batch_iterate(m16_batch *b, int32_t count, void *stream)
+{
+    if (!b || count < 0) return M16_ERR_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int k = 0; k < count && b->iterations_run < b->params.num_iter; ++k) {
+        const bool check = (b->iterations_run % b->params.update) == 0;
+        launch_iteration(b->B, b->seg, b->ninst, &b->params, st, check, nullptr, nullptr, nullptr);
+        ++b->iterations_run;
+    }
+    M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}
+
+extern "C" int m16_batch_end(m16_batch *b, int32_t *iterations, double *residuals, void *stream)
+{
+    if (!b) return M16_ERR_BAD_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = M16_OK;
+    for (int i = 0; i < b->ninst && rc == M16_OK; ++i) {
+        const int blocks = (int)std::min<int64_t>(kMaxBlocks, div_up(b->inst_n[i], 256));
+        bt_scatter_u_kernel<<<blocks, 256, 0, st>>>(b->B.dgroups, b->B.dinsts, i, b->inst_n[i]);
+        if (cudaGetLastError() != cudaSuccess) rc = M16_ERR_CUDA;
+    }
+    if (rc == M16_OK &&
+        (cudaMemcpyAsync(b->B.hctrl.data(), b->B.dctrl, sizeof(InstCtrl) * b->ninst, cudaMemcpyDeviceToHost, st) !=
+             cudaSuccess ||
+         cudaStreamSynchronize(st) != cudaSuccess))
+        rc = M16_ERR_CUDA;
+    if (rc == M16_OK) {
+        for (int i = 0; i < b->ninst; ++i) {
+            const InstCtrl &c = b->B.hctrl[i];
+            // an instance that never stopped ran every iteration enqueued
+            // directly or, replayed from graphs of whole check intervals, one
+            // check interval per check
+            const int ran = std::min(b->params.num_iter, std::max(b->iterations_run, c.n_checks * b->params.update));
+            if (iterations) iterations[i] = c.stopped ? c.iterations : ran;
+            if (residuals) residuals[i] = c.resid;
+        }
+    }
+    delete b;
+    return rc;
 }

@@ -235,3 +235,26 @@ def test_host_tree_helpers(lib):
     bad = np.array([0, 7], np.int32)
     assert lib.m16_tree_order(5, vp(bad), vp(bad), 2, 0, vp(order), vp(pred)) == N.M16_ERR_BAD_ARG
     assert lib.m16_tree_order(5, vp(ea), vp(eb), 3, 9, vp(order), vp(pred)) == N.M16_ERR_BAD_ARG
+
+
+def test_batch_steps_validate_before_touching_the_gpu(lib):
+    from miccai2016_gb300 import _native as N
+    fake = ctypes.c_void_p(256)
+    vd = (N.BatchVolume * 1)()
+    vd[0] = N.BatchVolume(8, 8, 8, 0, fake, fake, fake, fake, fake, (ctypes.c_double * 3)(1, 1, 1))
+    idesc = (N.BatchInstance * 1)()
+    idesc[0] = N.BatchInstance(0, 0, 0.1, 3.0, None, (ctypes.c_double * 3)(1, 1, 1), fake)
+    p = N.CutParams(0.2, 0.11, 1e-4, 100, 10, (ctypes.c_double * 3)(1, 1, 1))
+    h = ctypes.c_void_p()
+    nb = lib.m16_batch_workspace_bytes(vd, 1, idesc, 1)
+    assert nb > 0
+    assert lib.m16_batch_begin(vd, 1, idesc, 1, ctypes.byref(p), fake, nb - 1, None, ctypes.byref(h)) == \
+        N.M16_ERR_WORKSPACE and not h.value
+    bad = N.CutParams(0.2, 0.11, 1e-4, 100, 0, (ctypes.c_double * 3)(1, 1, 1))   # update 0
+    assert lib.m16_batch_begin(vd, 1, idesc, 1, ctypes.byref(bad), fake, nb, None, ctypes.byref(h)) == \
+        N.M16_ERR_BAD_ARG
+    assert lib.m16_batch_begin(vd, 0, idesc, 1, ctypes.byref(p), fake, nb, None, ctypes.byref(h)) == \
+        N.M16_ERR_BAD_ARG
+    assert lib.m16_batch_begin(vd, 1, idesc, 1, ctypes.byref(p), fake, nb, None, None) == N.M16_ERR_BAD_ARG
+    assert lib.m16_batch_iterate(None, 5, None) == N.M16_ERR_BAD_ARG
+    assert lib.m16_batch_end(None, None, None, None) == N.M16_ERR_BAD_ARG

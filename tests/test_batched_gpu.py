@@ -176,3 +176,61 @@ def test_tuning_graphs_and_a_shrinking_work_list_together():
         assert abs(int(its[k]) - it) <= 10
         if int(its[k]) == it:
             assert np.max(np.abs(us[k] - u)) <= U_TOL
+
+
+def _steps_batch():
+    vols = [_volume(21, (30, 26, 40)), _volume(22, (19, 35, 12))]
+    insts = [dict(volume=0, weighting=10 ** -1.25, decay=10 ** 1.5, eigs=ATV),
+             dict(volume=0, weighting=0.02, decay=3.0, eigs=ATV),
+             dict(volume=0, weighting=0.3, decay=0.7, eigs=ATV),
+             dict(volume=0, weighting=0.1, decay=30.0, eigs=ATV),      # one four-lane group
+             dict(volume=1, weighting=0.05, decay=5.0, eigs=TV),       # one-lane groups
+             dict(volume=1, alpha=np.full((19, 35, 12), 0.07, np.float32), eigs=ATV)]
+    return vols, insts
+
+
+def _cut(num_iter, update, error_bound):
+    from miccai2016_gb300.batched import BatchedCut
+    p = BatchedCut.CutParameters()
+    p.num_iter, p.update, p.error_bound = num_iter, update, error_bound
+    return BatchedCut(p)
+
+
+def test_steps_equal_the_whole_solve():
+    """m16_batch_begin / iterate (in uneven pieces) / end give the bits and
+    iteration counts of m16_batch_solve with the default tile shape."""
+    vols, insts = _steps_batch()
+    b = _cut(300, 30, 1e-3)
+    dv = [b.prepare_volume(v["img"], v["quats"], v["cs"], v["ct"], grad2=v["grad2"]) for v in vols]
+    ref = [u.cpu().numpy() for u in b.solve(dv, insts, tune=False, graphs=False)]
+    ref_its = b.last_iterations.copy()
+    assert ref_its.min() < 300   # some instances stop on their own
+    steps = b.begin(dv, insts)
+    for count in (7, 23, 45, 1, 100, 200):   # 376 requested: bounded by num_iter
+        steps.iterate(count)
+    us = [u.cpu().numpy() for u in steps.end()]
+    assert np.array_equal(steps.iterations, ref_its)
+    for u, r in zip(us, ref):
+        assert np.array_equal(u.view(np.uint32), r.view(np.uint32))
+
+
+def test_steps_replayed_from_a_cuda_graph():
+    """One check interval captured into a CUDA graph and replayed gives the
+    bits of the direct solve."""
+    import torch
+    vols, insts = _steps_batch()
+    b = _cut(120, 30, -1.0)
+    dv = [b.prepare_volume(v["img"], v["quats"], v["cs"], v["ct"], grad2=v["grad2"]) for v in vols]
+    ref = [u.cpu().numpy() for u in b.solve(dv, insts, tune=False, graphs=False)]
+    steps = b.begin(dv, insts)
+    steps.iterate(30)                        # iterations 0..29 directly
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        steps.iterate(30)                    # captured: one interval with its check first
+    for _ in range(3):                       # iterations 30..119
+        g.replay()
+    us = [u.cpu().numpy() for u in steps.end()]
+    assert np.all(steps.iterations == 120)
+    for u, r in zip(us, ref):
+        assert np.array_equal(u.view(np.uint32), r.view(np.uint32))
