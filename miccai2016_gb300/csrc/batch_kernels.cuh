@@ -407,16 +407,24 @@ __global__ void __launch_bounds__(kTile, M16_BATCH_MINB) bt_label_kernel(const i
 #ifndef M16_BATCH1_MINB
 #define M16_BATCH1_MINB 4
 #endif
-// z-slices whose loads the one-lane flow / label sweeps issue together:
-// measured on GB300 for one 256^3 instance of 1000 iterations, flow 1 /
-// label 4 takes 259 ms (alpha field: 257 ms), flow 2 / label 4 264 (285),
-// flow 1 / label 2 293 (291), flow 2 / label 2 297 (319); the single solve's
-// own sweeps take 232 ms
+// z-slices whose loads the one-lane flow / label sweeps issue together, and
+// whether the flow sweep reads its view (the descriptor values) from shared
+// memory.  Measured on GB300 for one 256^3 instance of 1000 iterations (with
+// an alpha field in brackets), the single solve's own sweeps taking 232 ms:
+//   view in registers: flow 1 / label 4 259 (257) ms, flow 2 / label 4 264
+//   (285), flow 1 / label 2 293 (291), flow 2 / label 2 297 (319);
+//   flow view in shared memory, flow 2 / label 4: 245 (243) ms; both views in
+//   shared memory, flow 2 / label 2: 258 (256).
 #ifndef M16_BATCH1_FZB
-#define M16_BATCH1_FZB 1
+#define M16_BATCH1_FZB 2
 #endif
 #ifndef M16_BATCH1_UZB
 #define M16_BATCH1_UZB M16_MF_UZB
+#endif
+// bit 1: the one-lane flow sweep reads its view from shared memory, bit 2:
+// the label sweep does
+#ifndef M16_BATCH1_SMEM_VIEW
+#define M16_BATCH1_SMEM_VIEW 1
 #endif
 
 template <int ALPHA>
@@ -431,6 +439,32 @@ __global__ void __launch_bounds__(kTile, M16_BATCH1_MINB) bt1_flow_kernel(const 
     int bx, by, bz;
     decode_tile(V, wk.y, bx, by, bz);
     const int x = bx * kBX + threadIdx.x, y = by * kBY + threadIdx.y;
+#if (M16_BATCH1_SMEM_VIEW & 1)
+    // the view in shared memory: its fields are read where used instead of
+    // held in registers for the whole column
+    __shared__ FlowView sf;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        float *st = (float *)G.state;
+        const int64_t S = G.slab;
+        sf.d0 = V.d0; sf.d1 = V.d1; sf.d2 = V.d2;
+        sf.ss0 = V.ss0; sf.ss1 = V.ss1; sf.ss2 = V.ss2;
+        sf.sq0 = G.sq0; sf.sq1 = G.sq1; sf.sq2 = G.sq2; sf.isq0 = G.isq0; sf.isq1 = G.isq1; sf.isq2 = G.isq2;
+        sf.alpha_scalar = 0.f;
+        sf.alpha = G.alpha1;
+        sf.grad2 = V.grad2;
+        sf.w = G.w.x;
+        sf.neg_inv_decay2 = G.nid2.x;
+        sf.sqeigs = nullptr;
+        sf.q4 = V.q4;
+        sf.tmp = st + 4 * S;
+        sf.hp0 = st; sf.hp1 = st + S; sf.hp2 = st + 2 * S;
+    }
+    __syncthreads();
+    if (x >= sf.d2 || y >= sf.d1) return;
+    const int zc = V.zc;
+    const int z0 = bz * zc, z1 = min(z0 + zc, sf.d0);
+    flow_column<false, ALPHA, M16_BATCH1_FZB>(sf, x, y, z0, z1);
+#else
     if (x >= V.d2 || y >= V.d1) return;
     const int z0 = bz * V.zc, z1 = min(z0 + V.zc, V.d0);
     float *st = (float *)G.state;
@@ -449,6 +483,7 @@ __global__ void __launch_bounds__(kTile, M16_BATCH1_MINB) bt1_flow_kernel(const 
     f.tmp = st + 4 * S;
     f.hp0 = st; f.hp1 = st + S; f.hp2 = st + 2 * S;
     flow_column<false, ALPHA, M16_BATCH1_FZB>(f, x, y, z0, z1);
+#endif
 }
 
 template <bool CHECK>
@@ -467,6 +502,20 @@ __global__ void __launch_bounds__(kTile, M16_BATCH1_MINB) bt1_label_kernel(const
     const int x = bx * kBX + threadIdx.x, y = by * kBY + threadIdx.y;
     const int z0 = bz * V.zc, z1 = min(z0 + V.zc, V.d0);
     float acc = 0.f;
+#if (M16_BATCH1_SMEM_VIEW & 2)
+    __shared__ LabelView sl;   // read where used, not held in registers
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        float *st = (float *)G.state;
+        const int64_t S = G.slab;
+        sl.d0 = V.d0; sl.d1 = V.d1; sl.d2 = V.d2;
+        sl.rcc = V.rcc; sl.rs0 = V.rs0; sl.rs1 = V.rs1; sl.rs2 = V.rs2;
+        sl.hp0 = st; sl.hp1 = st + S; sl.hp2 = st + 2 * S;
+        sl.cs = V.cs; sl.ct = V.ct; sl.labels = nullptr;
+        sl.pt = st + 3 * S; sl.tmp = st + 4 * S; sl.u = st + 5 * S;
+    }
+    __syncthreads();
+    if (x < sl.d2 && y < sl.d1) acc = label_column<false, M16_BATCH1_UZB>(sl, x, y, z0, z1);
+#else
     if (x < V.d2 && y < V.d1) {
         float *st = (float *)G.state;
         const int64_t S = G.slab;
@@ -478,6 +527,7 @@ __global__ void __launch_bounds__(kTile, M16_BATCH1_MINB) bt1_label_kernel(const
         l.pt = st + 3 * S; l.tmp = st + 4 * S; l.u = st + 5 * S;
         acc = label_column<false, M16_BATCH1_UZB>(l, x, y, z0, z1);
     }
+#endif
     if (CHECK) {
         const int tid = threadIdx.x + kBX * threadIdx.y;
 #pragma unroll
