@@ -755,8 +755,8 @@ def run_paths(args, cfg):
     sq = (ctypes.c_double * 3)(*np.sqrt(P.ATV_EIGS).tolist())
     stream = torch.cuda.current_stream()
 
-    def solve(path, zc=0, timing=0):
-        s = N.SolveStats(timing, 0, 0, 0, 0.0, 0.0, path, 0)
+    def solve(path, zc=0, timing=0, flags=0):
+        s = N.SolveStats(timing, 0, 0, 0, 0.0, 0.0, path, flags)
         s.pair_zc = zc
         it = ctypes.c_int32(0)
         st = L.m16_maxflow_solve_ex(N.ptr(d["img"]), N.ptr(d["quats"]), sq, None, N.ptr(d["alpha"]), 0.0,
@@ -766,17 +766,17 @@ def run_paths(args, cfg):
         N.check("m16_maxflow_solve_ex", st)
         return s
 
-    def timed(path, zc=0):
+    def timed(path, zc=0, flags=0):
         for _ in range(args.warmup):
-            solve(path, zc)
+            solve(path, zc, flags=flags)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            s = solve(path, zc)
+            s = solve(path, zc, flags=flags)
         e1.record(stream)
         torch.cuda.synchronize()
-        k = solve(path, zc, timing=1)
+        k = solve(path, zc, timing=1, flags=flags)
         r = dict(ms_per_solve=e0.elapsed_time(e1) / args.steps, launches=s.launches,
                  iterations_not_in_pairs=k.p_launches)
         if path == N.PATH_PAIRS:
@@ -794,6 +794,8 @@ def run_paths(args, cfg):
     if "two_sweeps" in wanted:
         out["two_sweeps"] = timed(N.PATH_TWO_SWEEPS)
         u_ref = u.clone()
+        out["two_sweeps_no_pdl"] = timed(N.PATH_TWO_SWEEPS, flags=N.SOLVE_NO_PDL)
+        out["two_sweeps_no_pdl"]["max_u_diff_vs_pdl"] = float((u - u_ref).abs().max())
     if "fused" in wanted:
         out["fused"] = timed(N.PATH_FUSED)
     if "pairs" in wanted:

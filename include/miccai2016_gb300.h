@@ -134,6 +134,10 @@ typedef struct m16_solve_stats {
  * iterations of the solve) and keeps the fastest, later batches of that shape
  * reuse it.  Timed solves and batches too small to matter use the default. */
 #define M16_BATCH_NO_TUNE 2
+/* m16_solve_stats.flags: launch the single solve's sweeps in plain stream
+ * order instead of with programmatic dependent launch (where each sweep's grid
+ * is scheduled while the previous one drains and waits for it on the device). */
+#define M16_SOLVE_NO_PDL 4
 
 /* m16_maxflow_solve with counters; stats (host) may be NULL. */
 int m16_maxflow_solve_ex(const float *img, const float *quat3, const double *sqevals3,

@@ -55,6 +55,7 @@ PATH_DEFAULT, PATH_TWO_SWEEPS, PATH_FUSED, PATH_PAIRS = 0, 1, 2, 3
 
 BATCH_NO_GRAPH = 1   # m16_solve_stats.flags
 BATCH_NO_TUNE = 2
+SOLVE_NO_PDL = 4    # m16_solve_stats.flags: the single solve without programmatic dependent launch
 
 
 class SolveStats(ctypes.Structure):

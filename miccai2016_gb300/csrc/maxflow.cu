@@ -119,6 +119,17 @@ __global__ void mf_init_kernel(MfArgs a, const float *__restrict__ img, const fl
     }
 }
 
+// ---- programmatic dependent launch --------------------------------------------
+// The sweeps are launched with programmatic stream serialization: a sweep's
+// grid may be scheduled while the previous one's last blocks still run, and
+// each block waits (griddepcontrol.wait: until the previous grid has completed
+// and its memory is visible) before it reads anything.  Every block lets the
+// next grid launch as soon as it starts; the next grid is then launched once
+// every block of this one has started, so it never takes an SM slot that one
+// of this grid's blocks still needs.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_next() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
 // ---- P and U sweeps (bodies in sweeps.cuh, shared with the batched engine) --
 
 // resident blocks per SM the sweeps are compiled for: 4 caps them at 64
@@ -158,6 +169,8 @@ __device__ __forceinline__ LabelView label_view(const MfArgs &a)
 template <bool POINTWISE, bool ALPHA_ARR>
 __global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_p_kernel(MfArgs a)
 {
+    pdl_wait();
+    pdl_launch_next();
     if (__ldcg(&a.ctrl->stopped)) return;
     const int x = blockIdx.x * kBX + threadIdx.x;
     const int y = blockIdx.y * kBY + threadIdx.y;
@@ -170,6 +183,8 @@ template <bool SUPERVISED, bool CHECK>
 __global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_u_kernel(MfArgs a)
 {
     __shared__ float red[32];
+    pdl_wait();
+    pdl_launch_next();
     if (__ldcg(&a.ctrl->stopped)) return;
     const int x = blockIdx.x * kBX + threadIdx.x;
     const int y = blockIdx.y * kBY + threadIdx.y;
@@ -305,12 +320,32 @@ inline cudaError_t launch_pair(bool alpha_arr, bool sup, bool check, dim3 grid, 
                  : launch_pair_t<false, false, false>(grid, st, a, parity);
 }
 
+// a launch with programmatic stream serialization when pdl is set (the
+// kernel waits for its predecessor itself), a plain launch otherwise
+template <typename... KArgs, typename... Args>
+cudaError_t launch_sweep(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, bool pdl, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // residual = sum(partials) / (N * rcc); stop on NaN or below the bound
 // (continuous_cut_anisotropic_gpu.py:321-337)
 __global__ void mf_check_kernel(const float *__restrict__ part, int nparts, double inv_norm, double bound,
                                 int iter, int check_idx, int resid_cap, MfCtrl *ctrl, double *resid)
 {
     __shared__ double s[256];
+    pdl_wait();
+    pdl_launch_next();
     if (__ldcg(&ctrl->stopped)) return;
     double acc = 0.0;
     for (int k = threadIdx.x; k < nparts; k += blockDim.x) acc += (double)part[k];
@@ -537,6 +572,7 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
     const int chunk = update * std::max(1, 64 / update);
 
     const bool timing = stats && stats->time_kernels;
+    const bool pdl = !(stats && (stats->flags & M16_SOLVE_NO_PDL));
     std::unique_ptr<EventPool> pool;
     if (timing) {
         pool.reset(new EventPool(3 * chunk));
@@ -602,24 +638,25 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
             }
             const MfArgs &s = cur ? b : a;
             if (pointwise) {
-                if (alpha_arr) mf_update_p_kernel<true, true><<<grid, block, 0, st>>>(s);
-                else mf_update_p_kernel<true, false><<<grid, block, 0, st>>>(s);
+                if (alpha_arr) M16_CUDA_TRY(launch_sweep(mf_update_p_kernel<true, true>, grid, block, st, pdl, s));
+                else M16_CUDA_TRY(launch_sweep(mf_update_p_kernel<true, false>, grid, block, st, pdl, s));
             } else {
-                if (alpha_arr) mf_update_p_kernel<false, true><<<grid, block, 0, st>>>(s);
-                else mf_update_p_kernel<false, false><<<grid, block, 0, st>>>(s);
+                if (alpha_arr) M16_CUDA_TRY(launch_sweep(mf_update_p_kernel<false, true>, grid, block, st, pdl, s));
+                else M16_CUDA_TRY(launch_sweep(mf_update_p_kernel<false, false>, grid, block, st, pdl, s));
             }
             if (timing) cudaEventRecord(pool->ev[3 * j + 1], st);
             const bool check = (it % update) == 0;
             if (check) {
-                if (sup) mf_update_u_kernel<true, true><<<grid, block, 0, st>>>(s);
-                else mf_update_u_kernel<false, true><<<grid, block, 0, st>>>(s);
+                if (sup) M16_CUDA_TRY(launch_sweep(mf_update_u_kernel<true, true>, grid, block, st, pdl, s));
+                else M16_CUDA_TRY(launch_sweep(mf_update_u_kernel<false, true>, grid, block, st, pdl, s));
                 if (timing) cudaEventRecord(pool->ev[3 * j + 2], st);
-                mf_check_kernel<<<1, 256, 0, st>>>(a.partials, nparts_sweep, inv_norm, params->error_bound, it,
-                                                   it / update, L.resid_cap, a.ctrl, resid);
+                M16_CUDA_TRY(launch_sweep(mf_check_kernel, dim3(1), dim3(256), st, pdl, (const float *)a.partials,
+                                          nparts_sweep, inv_norm, params->error_bound, it, it / update, L.resid_cap,
+                                          a.ctrl, resid));
                 ++launches;
             } else {
-                if (sup) mf_update_u_kernel<true, false><<<grid, block, 0, st>>>(s);
-                else mf_update_u_kernel<false, false><<<grid, block, 0, st>>>(s);
+                if (sup) M16_CUDA_TRY(launch_sweep(mf_update_u_kernel<true, false>, grid, block, st, pdl, s));
+                else M16_CUDA_TRY(launch_sweep(mf_update_u_kernel<false, false>, grid, block, st, pdl, s));
                 if (timing) cudaEventRecord(pool->ev[3 * j + 2], st);
             }
             launches += 2;
