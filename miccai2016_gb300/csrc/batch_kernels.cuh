@@ -250,6 +250,8 @@ __global__ void __launch_bounds__(kTile, M16_BATCH_MINB) bt_flow_kernel(const in
                                                                        const VolDev *vols, const GroupDev *groups,
                                                                        const unsigned *__restrict__ gmask)
 {
+    pdl_wait();
+    pdl_launch_next();
     const int2 wk = work[blockIdx.x];
     if (__ldcg(gmask + wk.x) == kAllLanes) return;
     const GroupDev &G = groups[wk.x];
@@ -324,6 +326,8 @@ __global__ void __launch_bounds__(kTile, M16_BATCH_MINB) bt_label_kernel(const i
                                                                         const unsigned *__restrict__ gmask,
                                                                         float4 *__restrict__ partials)
 {
+    pdl_wait();
+    pdl_launch_next();
     __shared__ float4 red[kTile / 32];
     const int2 wk = work[blockIdx.x];
     const unsigned stopped = __ldcg(gmask + wk.x);
@@ -432,6 +436,8 @@ __global__ void __launch_bounds__(kTile, M16_BATCH1_MINB) bt1_flow_kernel(const 
                                                                          const VolDev *vols, const GroupDev *groups,
                                                                          const unsigned *__restrict__ gmask)
 {
+    pdl_wait();
+    pdl_launch_next();
     const int2 wk = work[blockIdx.x];
     if (__ldcg(gmask + wk.x) & 1u) return;
     const GroupDev &G = groups[wk.x];
@@ -492,6 +498,8 @@ __global__ void __launch_bounds__(kTile, M16_BATCH1_MINB) bt1_label_kernel(const
                                                                           const unsigned *__restrict__ gmask,
                                                                           float4 *__restrict__ partials)
 {
+    pdl_wait();
+    pdl_launch_next();
     __shared__ float red[kTile / 32];
     const int2 wk = work[blockIdx.x];
     if (__ldcg(gmask + wk.x) & 1u) return;   // uniform over the block
@@ -551,6 +559,8 @@ __global__ void bt_check_kernel(const VolDev *vols, const GroupDev *groups, cons
                                 InstCtrl *ctrl, unsigned *gmask, const float4 *__restrict__ partials, double bound,
                                 int update, const int *__restrict__ list)
 {
+    pdl_wait();
+    pdl_launch_next();
     __shared__ double s[256];
     const int inst = list ? list[blockIdx.x] : (int)blockIdx.x;   // list: the instances to check
     const InstDev &I = insts[inst];

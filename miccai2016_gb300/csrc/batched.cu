@@ -329,35 +329,47 @@ int launch_iteration(const BatchRun &B, const int *seg, int ninst, const m16_cut
     int n = 0;
     if (e0) cudaEventRecord(e0, s);
     const int n4 = seg[2], n1 = seg[4] - seg[2];
+    cudaError_t e = cudaSuccess;
+    auto keep = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
     if (seg[1] > seg[0])
-        bt_flow_kernel<true><<<seg[1] - seg[0], block, 0, s>>>(B.dwork + seg[0], B.dvols, B.dgroups, B.dmask);
+        keep(launch_pdl(bt_flow_kernel<true>, dim3(seg[1] - seg[0]), block, s, true, B.dwork + seg[0], B.dvols,
+                        B.dgroups, B.dmask));
     if (seg[2] > seg[1])
-        bt_flow_kernel<false><<<seg[2] - seg[1], block, 0, s>>>(B.dwork + seg[1], B.dvols, B.dgroups, B.dmask);
+        keep(launch_pdl(bt_flow_kernel<false>, dim3(seg[2] - seg[1]), block, s, true, B.dwork + seg[1], B.dvols,
+                        B.dgroups, B.dmask));
     if (seg[3] > seg[2])
-        bt1_flow_kernel<kAlphaArray><<<seg[3] - seg[2], block, 0, s>>>(B.dwork + seg[2], B.dvols, B.dgroups,
-                                                                        B.dmask);
+        keep(launch_pdl(bt1_flow_kernel<kAlphaArray>, dim3(seg[3] - seg[2]), block, s, true, B.dwork + seg[2],
+                        B.dvols, B.dgroups, B.dmask));
     if (seg[4] > seg[3])
-        bt1_flow_kernel<kAlphaFromGrad2><<<seg[4] - seg[3], block, 0, s>>>(B.dwork + seg[3], B.dvols, B.dgroups,
-                                                                            B.dmask);
+        keep(launch_pdl(bt1_flow_kernel<kAlphaFromGrad2>, dim3(seg[4] - seg[3]), block, s, true, B.dwork + seg[3],
+                        B.dvols, B.dgroups, B.dmask));
     if (e1) cudaEventRecord(e1, s);
     if (n4 > 0) {
-        if (check) bt_label_kernel<true><<<n4, block, 0, s>>>(B.dwork, B.dvols, B.dgroups, B.dmask, B.dpart);
-        else bt_label_kernel<false><<<n4, block, 0, s>>>(B.dwork, B.dvols, B.dgroups, B.dmask, B.dpart);
+        if (check)
+            keep(launch_pdl(bt_label_kernel<true>, dim3(n4), block, s, true, B.dwork, B.dvols, B.dgroups, B.dmask,
+                            B.dpart));
+        else
+            keep(launch_pdl(bt_label_kernel<false>, dim3(n4), block, s, true, B.dwork, B.dvols, B.dgroups, B.dmask,
+                            B.dpart));
     }
     if (n1 > 0) {
         if (check)
-            bt1_label_kernel<true><<<n1, block, 0, s>>>(B.dwork + seg[2], B.dvols, B.dgroups, B.dmask, B.dpart);
+            keep(launch_pdl(bt1_label_kernel<true>, dim3(n1), block, s, true, B.dwork + seg[2], B.dvols, B.dgroups,
+                            B.dmask, B.dpart));
         else
-            bt1_label_kernel<false><<<n1, block, 0, s>>>(B.dwork + seg[2], B.dvols, B.dgroups, B.dmask, B.dpart);
+            keep(launch_pdl(bt1_label_kernel<false>, dim3(n1), block, s, true, B.dwork + seg[2], B.dvols, B.dgroups,
+                            B.dmask, B.dpart));
     }
     if (e2) cudaEventRecord(e2, s);
     for (int k = 0; k < 4; ++k) n += seg[k + 1] > seg[k];
     n += (n4 > 0) + (n1 > 0);
     if (check) {
-        bt_check_kernel<<<ninst, 256, 0, s>>>(B.dvols, B.dgroups, B.dinsts, B.dctrl, B.dmask, B.dpart,
-                                              params->error_bound, params->update, nullptr);
+        keep(launch_pdl(bt_check_kernel, dim3(ninst), dim3(256), s, true, (const VolDev *)B.dvols,
+                        (const GroupDev *)B.dgroups, (const InstDev *)B.dinsts, B.dctrl, B.dmask,
+                        (const float4 *)B.dpart, params->error_bound, params->update, (const int *)nullptr));
         ++n;
     }
+    if (e != cudaSuccess) return -1;
     return n;
 }
 

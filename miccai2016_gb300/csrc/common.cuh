@@ -89,4 +89,36 @@ __device__ __forceinline__ float block_sum(float v, float *smem32)
     return r;
 }
 
+
+// ---- programmatic dependent launch --------------------------------------------
+// The iteration sweeps are launched with programmatic stream serialization: a
+// sweep's grid may be scheduled while the previous one's last blocks still
+// run, and each block waits (griddepcontrol.wait: until the previous grid has
+// completed and its memory is visible) before it reads anything.  Every block
+// lets the next grid launch as soon as it starts; the next grid is then
+// launched once every block of this one has started, so it never takes an SM
+// slot that one of this grid's blocks still needs.  Without the launch
+// attribute both instructions return at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_next() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+// a launch with programmatic stream serialization when pdl is set (the kernel
+// waits for its predecessor itself), a plain stream-ordered launch otherwise
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, bool pdl,
+                              Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 }  // namespace m16

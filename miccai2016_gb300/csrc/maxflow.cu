@@ -119,17 +119,6 @@ __global__ void mf_init_kernel(MfArgs a, const float *__restrict__ img, const fl
     }
 }
 
-// ---- programmatic dependent launch --------------------------------------------
-// The sweeps are launched with programmatic stream serialization: a sweep's
-// grid may be scheduled while the previous one's last blocks still run, and
-// each block waits (griddepcontrol.wait: until the previous grid has completed
-// and its memory is visible) before it reads anything.  Every block lets the
-// next grid launch as soon as it starts; the next grid is then launched once
-// every block of this one has started, so it never takes an SM slot that one
-// of this grid's blocks still needs.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
-__device__ __forceinline__ void pdl_launch_next() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
-
 // ---- P and U sweeps (bodies in sweeps.cuh, shared with the batched engine) --
 
 // resident blocks per SM the sweeps are compiled for: 4 caps them at 64
@@ -318,24 +307,6 @@ inline cudaError_t launch_pair(bool alpha_arr, bool sup, bool check, dim3 grid, 
                           : launch_pair_t<false, true, false>(grid, st, a, parity);
     return check ? launch_pair_t<false, false, true>(grid, st, a, parity)
                  : launch_pair_t<false, false, false>(grid, st, a, parity);
-}
-
-// a launch with programmatic stream serialization when pdl is set (the
-// kernel waits for its predecessor itself), a plain launch otherwise
-template <typename... KArgs, typename... Args>
-cudaError_t launch_sweep(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, bool pdl, Args... args)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
 // residual = sum(partials) / (N * rcc); stop on NaN or below the bound
@@ -638,25 +609,25 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
             }
             const MfArgs &s = cur ? b : a;
             if (pointwise) {
-                if (alpha_arr) M16_CUDA_TRY(launch_sweep(mf_update_p_kernel<true, true>, grid, block, st, pdl, s));
-                else M16_CUDA_TRY(launch_sweep(mf_update_p_kernel<true, false>, grid, block, st, pdl, s));
+                if (alpha_arr) M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<true, true>, grid, block, st, pdl, s));
+                else M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<true, false>, grid, block, st, pdl, s));
             } else {
-                if (alpha_arr) M16_CUDA_TRY(launch_sweep(mf_update_p_kernel<false, true>, grid, block, st, pdl, s));
-                else M16_CUDA_TRY(launch_sweep(mf_update_p_kernel<false, false>, grid, block, st, pdl, s));
+                if (alpha_arr) M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<false, true>, grid, block, st, pdl, s));
+                else M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<false, false>, grid, block, st, pdl, s));
             }
             if (timing) cudaEventRecord(pool->ev[3 * j + 1], st);
             const bool check = (it % update) == 0;
             if (check) {
-                if (sup) M16_CUDA_TRY(launch_sweep(mf_update_u_kernel<true, true>, grid, block, st, pdl, s));
-                else M16_CUDA_TRY(launch_sweep(mf_update_u_kernel<false, true>, grid, block, st, pdl, s));
+                if (sup) M16_CUDA_TRY(launch_pdl(mf_update_u_kernel<true, true>, grid, block, st, pdl, s));
+                else M16_CUDA_TRY(launch_pdl(mf_update_u_kernel<false, true>, grid, block, st, pdl, s));
                 if (timing) cudaEventRecord(pool->ev[3 * j + 2], st);
-                M16_CUDA_TRY(launch_sweep(mf_check_kernel, dim3(1), dim3(256), st, pdl, (const float *)a.partials,
+                M16_CUDA_TRY(launch_pdl(mf_check_kernel, dim3(1), dim3(256), st, pdl, (const float *)a.partials,
                                           nparts_sweep, inv_norm, params->error_bound, it, it / update, L.resid_cap,
                                           a.ctrl, resid));
                 ++launches;
             } else {
-                if (sup) M16_CUDA_TRY(launch_sweep(mf_update_u_kernel<true, false>, grid, block, st, pdl, s));
-                else M16_CUDA_TRY(launch_sweep(mf_update_u_kernel<false, false>, grid, block, st, pdl, s));
+                if (sup) M16_CUDA_TRY(launch_pdl(mf_update_u_kernel<true, false>, grid, block, st, pdl, s));
+                else M16_CUDA_TRY(launch_pdl(mf_update_u_kernel<false, false>, grid, block, st, pdl, s));
                 if (timing) cudaEventRecord(pool->ev[3 * j + 2], st);
             }
             launches += 2;

@@ -554,15 +554,22 @@ extern "C" int m16_server_step(m16_server *s)
         const dim3 block(kBX, kBY, 1);
         const int na = s->seg_alpha, ne = s->n_items - s->seg_alpha;
         M16_CUDA_TRY(cudaEventRecord(s->t_start[b], st));
+        // programmatic dependent launch between the sweeps (common.cuh); the
+        // first sweep follows an event record and launches in stream order
         for (int i = 0; i < s->params.update; ++i) {
-            if (na > 0) bt1_flow_kernel<kAlphaArray><<<na, block, 0, st>>>(dwork, dvols, dgroups, dmask);
-            if (ne > 0) bt1_flow_kernel<kAlphaFromGrad2><<<ne, block, 0, st>>>(dwork + na, dvols, dgroups, dmask);
+            if (na > 0) M16_CUDA_TRY(launch_pdl(bt1_flow_kernel<kAlphaArray>, dim3(na), block, st, true, dwork, dvols,
+                                                dgroups, (const unsigned *)dmask));
+            if (ne > 0) M16_CUDA_TRY(launch_pdl(bt1_flow_kernel<kAlphaFromGrad2>, dim3(ne), block, st, true,
+                                                dwork + na, dvols, dgroups, (const unsigned *)dmask));
             if (i == 0) {
-                bt1_label_kernel<true><<<s->n_items, block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
-                bt_check_kernel<<<s->n_list, 256, 0, st>>>(dvols, dgroups, dinsts, dctrl, dmask, dpart,
-                                                           s->params.error_bound, s->params.update, dlist);
+                M16_CUDA_TRY(launch_pdl(bt1_label_kernel<true>, dim3(s->n_items), block, st, true, dwork, dvols,
+                                        dgroups, (const unsigned *)dmask, dpart));
+                M16_CUDA_TRY(launch_pdl(bt_check_kernel, dim3(s->n_list), dim3(256), st, true, dvols, dgroups,
+                                        dinsts, dctrl, dmask, (const float4 *)dpart, s->params.error_bound,
+                                        s->params.update, dlist));
             } else {
-                bt1_label_kernel<false><<<s->n_items, block, 0, st>>>(dwork, dvols, dgroups, dmask, dpart);
+                M16_CUDA_TRY(launch_pdl(bt1_label_kernel<false>, dim3(s->n_items), block, st, true, dwork, dvols,
+                                        dgroups, (const unsigned *)dmask, dpart));
             }
         }
         M16_CUDA_TRY(cudaGetLastError());
