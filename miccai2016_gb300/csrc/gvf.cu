@@ -78,6 +78,8 @@ template <bool RESP, bool CHECK>
 __global__ void __launch_bounds__(kBX * kBY, M16_GVF_MINB) gvf_sweep_kernel(GvfArgs a)
 {
     __shared__ float red[32];
+    pdl_wait();          // programmatic dependent launch (common.cuh)
+    pdl_launch_next();
     if (__ldcg(&a.ctrl->stopped)) return;
     const int x = blockIdx.x * kBX + threadIdx.x;
     const int y = blockIdx.y * kBY + threadIdx.y;
@@ -160,6 +162,8 @@ __global__ void gvf_check_kernel(const float *__restrict__ part, int nparts, dou
                                  int check_idx, int cap, GvfCtrl *ctrl, double *mags)
 {
     __shared__ double s[256];
+    pdl_wait();
+    pdl_launch_next();
     if (__ldcg(&ctrl->stopped)) return;
     double acc = 0.0;
     for (int k = threadIdx.x; k < nparts; k += blockDim.x) acc += (double)part[k];
@@ -293,14 +297,16 @@ extern "C" int m16_gvf_run(const float *v3, const float *response, int32_t d0, i
         a.gi0 = in; a.gi1 = in + n; a.gi2 = in + 2 * n;
         a.go0 = out; a.go1 = out + n; a.go2 = out + 2 * n;
         const bool check = (it % update) == 0;
+        // programmatic dependent launch: each sweep waits on the device for
+        // the previous one (which reads the buffer it writes) before any access
         if (check) {
-            if (response) gvf_sweep_kernel<true, true><<<grid, block, 0, st>>>(a);
-            else gvf_sweep_kernel<false, true><<<grid, block, 0, st>>>(a);
-            gvf_check_kernel<<<1, 256, 0, st>>>(a.partials, L.nparts, inv_n, tol, it, it / update, L.cap, ctrl,
-                                                mlog);
+            if (response) M16_CUDA_TRY(launch_pdl(gvf_sweep_kernel<true, true>, grid, block, st, true, a));
+            else M16_CUDA_TRY(launch_pdl(gvf_sweep_kernel<false, true>, grid, block, st, true, a));
+            M16_CUDA_TRY(launch_pdl(gvf_check_kernel, dim3(1), dim3(256), st, true, (const float *)a.partials,
+                                    L.nparts, inv_n, tol, it, it / update, L.cap, ctrl, mlog));
         } else {
-            if (response) gvf_sweep_kernel<true, false><<<grid, block, 0, st>>>(a);
-            else gvf_sweep_kernel<false, false><<<grid, block, 0, st>>>(a);
+            if (response) M16_CUDA_TRY(launch_pdl(gvf_sweep_kernel<true, false>, grid, block, st, true, a));
+            else M16_CUDA_TRY(launch_pdl(gvf_sweep_kernel<false, false>, grid, block, st, true, a));
         }
     }
     M16_CUDA_TRY(cudaGetLastError());
