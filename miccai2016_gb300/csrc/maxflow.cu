@@ -561,7 +561,6 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
     int it = 0;
     while (it < params->num_iter) {
         const int end = std::min(params->num_iter, it + chunk);
-        const int first = it;
         // per launch slot: (start iteration, kind 0 sweeps / 1 pair), for the timing
         std::vector<int> slot_it, slot_kind;
         while (it < end) {
@@ -655,7 +654,6 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
                 }
             }
         }
-        (void)first;
         if (hctrl.stopped) break;
     }
     M16_CUDA_TRY(cudaMemcpyAsync(&hctrl, a.ctrl, sizeof(MfCtrl), cudaMemcpyDeviceToHost, st));
