@@ -73,6 +73,11 @@ __global__ void gvf_init_kernel(const float *__restrict__ v3, const float *__res
 #define M16_GVF_MINB 4   // 4 blocks per SM caps the sweep at 64 registers: measured fastest on GB300
 #endif
 constexpr int kGvfZB = M16_GVF_ZB;
+// 1: the x neighbours come from the adjacent lanes (warp shuffles) instead of
+// loads, except at the warp's ends
+#ifndef M16_GVF_XSHFL
+#define M16_GVF_XSHFL 0
+#endif
 
 template <bool RESP, bool CHECK>
 __global__ void __launch_bounds__(kBX * kBY, M16_GVF_MINB) gvf_sweep_kernel(GvfArgs a)
@@ -84,6 +89,10 @@ __global__ void __launch_bounds__(kBX * kBY, M16_GVF_MINB) gvf_sweep_kernel(GvfA
     const int x = blockIdx.x * kBX + threadIdx.x;
     const int y = blockIdx.y * kBY + threadIdx.y;
     float acc = 0.f;
+#if M16_GVF_XSHFL
+    const int lane = threadIdx.x;   // a warp is one 32-wide row of x (kBX = 32)
+    const unsigned active = __ballot_sync(0xffffffffu, x < a.d2 && y < a.d1);
+#endif
     if (x < a.d2 && y < a.d1) {
         const int z0 = blockIdx.z * a.zc;
         const int z1 = min(z0 + a.zc, a.d0);
@@ -114,8 +123,14 @@ __global__ void __launch_bounds__(kBX * kBY, M16_GVF_MINB) gvf_sweep_kernel(GvfA
                     if (z < a.d0 - 1) ld3(j + s0, nx[k][0], nx[k][1], nx[k][2]);   // z + 1
                     ld3(j + yb, nyb[k][0], nyb[k][1], nyb[k][2]);
                     ld3(j + ya, nya[k][0], nya[k][1], nya[k][2]);
+#if M16_GVF_XSHFL
+                    // only the warp's end lanes load their outer x neighbour
+                    if (lane == 0 && x > 0) ld3(j - 1, nxb[k][0], nxb[k][1], nxb[k][2]);
+                    if (lane == 31 && x < a.d2 - 1) ld3(j + 1, nxa[k][0], nxa[k][1], nxa[k][2]);
+#else
                     ld3(j + xb, nxb[k][0], nxb[k][1], nxb[k][2]);
                     ld3(j + xa, nxa[k][0], nxa[k][1], nxa[k][2]);
+#endif
                     w[k][0] = __ldg(a.v0 + j); w[k][1] = __ldg(a.v1 + j); w[k][2] = __ldg(a.v2 + j);
                     if (RESP) rr[k] = __ldg(a.r + j);
                 }
@@ -129,6 +144,27 @@ __global__ void __launch_bounds__(kBX * kBY, M16_GVF_MINB) gvf_sweep_kernel(GvfA
                     if (a.d0 == 1) { n0 = c0; n1 = c1; n2 = c2; }
                     else if (z < a.d0 - 1) { n0 = nx[k][0]; n1 = nx[k][1]; n2 = nx[k][2]; }
                     else { n0 = p0; n1 = p1; n2 = p2; }
+#if M16_GVF_XSHFL
+                    {
+                        // x - 1 and x + 1 from the neighbouring lanes (the active
+                        // lanes of a warp are 0 .. last, all in this branch)
+                        const float cc[3] = {c0, c1, c2};
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            const float up = __shfl_up_sync(active, cc[q], 1);     // x - 1
+                            const float dn = __shfl_down_sync(active, cc[q], 1);   // x + 1 (unused past the end)
+                            float xbv, xav;
+                            if (a.d2 == 1) { xbv = cc[q]; xav = cc[q]; }
+                            else {
+                                xbv = x == 0 ? dn : (lane == 0 ? nxb[k][q] : up);          // mirror at x = 0
+                                xav = x == a.d2 - 1 ? (lane == 0 ? nxb[k][q] : up)          // mirror at the end
+                                                    : (lane == 31 ? nxa[k][q] : dn);
+                            }
+                            nxb[k][q] = xbv;
+                            nxa[k][q] = xav;
+                        }
+                    }
+#endif
                     const float l0 = ((p0 + n0 - 2.f * c0) * a.rss0 + (nyb[k][0] + nya[k][0] - 2.f * c0) * a.rss1) +
                                      (nxb[k][0] + nxa[k][0] - 2.f * c0) * a.rss2;
                     const float l1 = ((p1 + n1 - 2.f * c1) * a.rss0 + (nyb[k][1] + nya[k][1] - 2.f * c1) * a.rss1) +
