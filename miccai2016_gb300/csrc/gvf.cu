@@ -74,7 +74,8 @@ __global__ void gvf_init_kernel(const float *__restrict__ v3, const float *__res
 #endif
 constexpr int kGvfZB = M16_GVF_ZB;
 // 1: the x neighbours come from the adjacent lanes (warp shuffles) instead of
-// loads, except at the warp's ends
+// loads, except at the warp's ends.  Measured slower on GB300 (256^3, 100
+// iterations: 12.64 ms against 12.27 ms with the loads, which hit L1), so off.
 #ifndef M16_GVF_XSHFL
 #define M16_GVF_XSHFL 0
 #endif
