@@ -162,6 +162,8 @@ class BatchSteps(object):
     def end(self):
         """u of every instance (CUDA tensors, instance order); sets
         .iterations and .residuals."""
+        if self._h is None:
+            raise RuntimeError("the batch has ended")
         its = (ctypes.c_int32 * self._n)()
         res = (ctypes.c_double * self._n)()
         h, self._h = self._h, None
@@ -169,6 +171,16 @@ class BatchSteps(object):
         self.iterations = np.array(its[:], np.int64)
         self.residuals = np.array(res[:], np.float64)
         return self._us
+
+    def __del__(self):
+        # a batch dropped without end(): finish it (m16_batch_end waits for
+        # its work) before the workspace goes back to the allocator
+        try:
+            if getattr(self, "_h", None) is not None:
+                h, self._h = self._h, None
+                self._L.m16_batch_end(h, None, None, N.stream_ptr())
+        except Exception:
+            pass
 
 
 def _main(argv=None):
