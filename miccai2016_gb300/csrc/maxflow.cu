@@ -52,8 +52,6 @@ struct MfArgs {
     float *hpB0, *hpB1, *hpB2, *tmpB;   // second ping-pong set of the fused iteration
     float *ptB, *uB;                    // with hpB, tmpB: the second state set of the pair kernel
     const float4 *q4;
-    float *qa, *qb, *qc;                // the quaternion in 12 bytes (q3_encode), when q3 is set
-    int q3;                             // the two-sweep path: quaternions in the 12-byte encoding
     const float *alpha, *sqeigs, *cs, *ct;
     const uint8_t *labels;
     float *partials;
@@ -104,8 +102,7 @@ __global__ void mf_init_ctrl_kernel(const float *__restrict__ part, int nparts, 
 }
 
 // hp = 0, p_t = fmin(cs, ct), u = img / denom, tmp = -u * rcc, q4 = qexpand(quat3)
-// (continuous_cut_anisotropic_gpu.py:276-289), or its 12-byte encoding for
-// the two sweeps
+// (continuous_cut_anisotropic_gpu.py:276-289)
 __global__ void mf_init_kernel(MfArgs a, const float *__restrict__ img, const float *__restrict__ quat3, int64_t n)
 {
     const float denom = a.ctrl->denom;
@@ -118,9 +115,7 @@ __global__ void mf_init_kernel(MfArgs a, const float *__restrict__ img, const fl
         a.u[i] = ui;
         a.tmp[i] = -(ui * a.rcc);
         const float *s = quat3 + 3 * i;
-        const float4 q = qexpand(s[0], s[1], s[2]);
-        if (a.q3) q3_encode(q, a.qa[i], a.qb[i], a.qc[i]);
-        else const_cast<float4 *>(a.q4)[i] = q;
+        const_cast<float4 *>(a.q4)[i] = qexpand(s[0], s[1], s[2]);
     }
 }
 
@@ -146,8 +141,7 @@ __device__ __forceinline__ FlowView flow_view(const MfArgs &a)
     f.ss0 = a.ss0; f.ss1 = a.ss1; f.ss2 = a.ss2;
     f.sq0 = a.sq0; f.sq1 = a.sq1; f.sq2 = a.sq2; f.isq0 = a.isq0; f.isq1 = a.isq1; f.isq2 = a.isq2;
     f.alpha_scalar = a.alpha_scalar; f.alpha = a.alpha; f.grad2 = nullptr; f.w = 0.f; f.neg_inv_decay2 = 0.f;
-    f.sqeigs = a.sqeigs; f.q4 = a.q4; f.qa = a.qa; f.qb = a.qb; f.qc = a.qc;
-    f.tmp = a.tmp; f.hp0 = a.hp0; f.hp1 = a.hp1; f.hp2 = a.hp2;
+    f.sqeigs = a.sqeigs; f.q4 = a.q4; f.tmp = a.tmp; f.hp0 = a.hp0; f.hp1 = a.hp1; f.hp2 = a.hp2;
     return f;
 }
 
@@ -161,9 +155,7 @@ __device__ __forceinline__ LabelView label_view(const MfArgs &a)
     return l;
 }
 
-// Q3: the quaternions in the 12-byte encoding (the two-sweep path), else
-// expanded (the pair path's single iterations)
-template <bool POINTWISE, bool ALPHA_ARR, bool Q3>
+template <bool POINTWISE, bool ALPHA_ARR>
 __global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_p_kernel(MfArgs a)
 {
     pdl_wait();
@@ -173,8 +165,7 @@ __global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_p_kernel(MfA
     const int y = blockIdx.y * kBY + threadIdx.y;
     if (x >= a.d2 || y >= a.d1) return;
     const int z0 = blockIdx.z * a.zc;
-    flow_column<POINTWISE, ALPHA_ARR ? kAlphaArray : kAlphaScalar, kMfZB, Q3>(flow_view(a), x, y, z0,
-                                                                             min(z0 + a.zc, a.d0));
+    flow_column<POINTWISE, ALPHA_ARR ? kAlphaArray : kAlphaScalar>(flow_view(a), x, y, z0, min(z0 + a.zc, a.d0));
 }
 
 template <bool SUPERVISED, bool CHECK>
@@ -521,12 +512,6 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
     a.ptB = pairs ? (float *)(ws + L.ptB) : nullptr;
     a.uB = pairs ? (float *)(ws + L.uB) : nullptr;
     a.q4 = (const float4 *)(ws + L.q4);
-    // the two sweeps read the quaternion in 12 bytes; the same region holds
-    // the three planar arrays (12 N of its 16 N bytes)
-    a.q3 = path == kSetsSweeps ? 1 : 0;
-    a.qa = (float *)(ws + L.q4);
-    a.qb = a.qa + n;
-    a.qc = a.qb + n;
     a.alpha = alpha; a.sqeigs = sqeigs; a.cs = cs; a.ct = ct; a.labels = labels;
     a.partials = (float *)(ws + L.partials);
     a.ctrl = (MfCtrl *)(ws + L.ctrl);
@@ -622,22 +607,12 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
                 continue;
             }
             const MfArgs &s = cur ? b : a;
-            if (a.q3) {
-                if (pointwise) {
-                    if (alpha_arr) M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<true, true, true>, grid, block, st, pdl, s));
-                    else M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<true, false, true>, grid, block, st, pdl, s));
-                } else {
-                    if (alpha_arr) M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<false, true, true>, grid, block, st, pdl, s));
-                    else M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<false, false, true>, grid, block, st, pdl, s));
-                }
+            if (pointwise) {
+                if (alpha_arr) M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<true, true>, grid, block, st, pdl, s));
+                else M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<true, false>, grid, block, st, pdl, s));
             } else {
-                if (pointwise) {
-                    if (alpha_arr) M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<true, true, false>, grid, block, st, pdl, s));
-                    else M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<true, false, false>, grid, block, st, pdl, s));
-                } else {
-                    if (alpha_arr) M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<false, true, false>, grid, block, st, pdl, s));
-                    else M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<false, false, false>, grid, block, st, pdl, s));
-                }
+                if (alpha_arr) M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<false, true>, grid, block, st, pdl, s));
+                else M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<false, false>, grid, block, st, pdl, s));
             }
             if (timing) cudaEventRecord(pool->ev[3 * j + 1], st);
             const bool check = (it % update) == 0;

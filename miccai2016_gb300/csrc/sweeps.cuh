@@ -39,46 +39,9 @@ struct FlowView {
     float w, neg_inv_decay2;
     const float *sqeigs;                       // per-voxel sqrt eigenvalues (POINTWISE)
     const float4 *q4;                          // expanded quaternions
-    const float *qa, *qb, *qc;                 // or their three smaller components (q3_encode)
     const float *tmp;
     float *hp0, *hp1, *hp2;
 };
-
-// A unit quaternion in 12 bytes ("smallest three"): q and -q give the same
-// rotation (quat2rot is quadratic in q, and negation is exact), so q is
-// negated until its largest-magnitude component m is positive; the other
-// three are stored in order, with m in the two low mantissa bits of the first
-// (a change of at most 3 ulp).  The decoder recovers the largest component as
-// sqrt(1 - a^2 - b^2 - c^2), which is at least 1/2, so the square root is
-// well conditioned: the rotation agrees with the expanded quaternion's to
-// about 1e-7.
-__device__ __forceinline__ void q3_encode(float4 q, float &a, float &b, float &c)
-{
-    const float v[4] = {q.x, q.y, q.z, q.w};
-    int m = 0;
-#pragma unroll
-    for (int k = 1; k < 4; ++k)
-        if (fabsf(v[k]) > fabsf(v[m])) m = k;
-    const float sg = v[m] < 0.f ? -1.f : 1.f;
-    float r[3];
-    int n = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-        if (k != m) r[n++] = sg * v[k];
-    a = __uint_as_float((__float_as_uint(r[0]) & ~3u) | (unsigned)m);
-    b = r[1];
-    c = r[2];
-}
-
-__device__ __forceinline__ float4 q3_decode(float a, float b, float c)
-{
-    const unsigned m = __float_as_uint(a) & 3u;
-    const float l = sqrtf(fmaxf(0.f, 1.f - (a * a + b * b + c * c)));
-    return m == 0 ? make_float4(l, a, b, c)
-           : m == 1 ? make_float4(a, l, b, c)
-           : m == 2 ? make_float4(a, b, l, c)
-                    : make_float4(a, b, c, l);
-}
 
 // Everything one instance's label sweep reads and writes.
 struct LabelView {
@@ -145,7 +108,7 @@ __device__ __forceinline__ float label_point(float rcc, float rs0, float rs1, fl
 
 // P: p = H^-1 hp + H^T (steps grad tmp), projected onto |p| <= alpha, hp = H p
 // (update_qp.cl:150-232) for voxels (z0..z1, y, x).
-template <bool POINTWISE, int ALPHA, int kFZB = kMfZB, bool Q3 = false>
+template <bool POINTWISE, int ALPHA, int kFZB = kMfZB>
 __device__ __forceinline__ void flow_column(const FlowView &a, int x, int y, int z0, int z1)
 {
     const int64_t s0 = (int64_t)a.d1 * a.d2;
@@ -163,8 +126,7 @@ __device__ __forceinline__ void flow_column(const FlowView &a, int x, int y, int
                 tz[k] = (zb + k < a.d0 - 1) ? __ldg(a.tmp + j + s0) : 0.f;
                 ty[k] = yin ? __ldg(a.tmp + j + a.d2) : 0.f;
                 tx[k] = xin ? __ldg(a.tmp + j + 1) : 0.f;
-                if (Q3) q[k] = make_float4(__ldg(a.qa + j), __ldg(a.qb + j), __ldg(a.qc + j), 0.f);
-                else q[k] = __ldg(a.q4 + j);
+                q[k] = __ldg(a.q4 + j);
                 if (ALPHA == kAlphaArray) al[k] = __ldg(a.alpha + j);
                 else if (ALPHA == kAlphaFromGrad2) al[k] = __ldg(a.grad2 + j);
                 else al[k] = a.alpha_scalar;
@@ -190,8 +152,7 @@ __device__ __forceinline__ void flow_column(const FlowView &a, int x, int y, int
                     i0v = 1.f / s0v; i1v = 1.f / s1v; i2v = 1.f / s2v;
                 }
                 const float rad = ALPHA == kAlphaFromGrad2 ? a.w * expf(a.neg_inv_decay2 * al[k]) : al[k];
-                const float4 qk = Q3 ? q3_decode(q[k].x, q[k].y, q[k].z) : q[k];
-                const float3 h = flow_point(a.ss0, a.ss1, a.ss2, tc, tz[k], ty[k], tx[k], zin, yin, xin, qk, rad,
+                const float3 h = flow_point(a.ss0, a.ss1, a.ss2, tc, tz[k], ty[k], tx[k], zin, yin, xin, q[k], rad,
                                             h0[k], h1[k], h2[k], s0v, s1v, s2v, i0v, i1v, i2v);
                 a.hp0[j] = h.x;
                 a.hp1[j] = h.y;
