@@ -32,7 +32,8 @@ extern "C" {
 #define M16_ERR_WORKSPACE 3     /* workspace NULL, misaligned or smaller than required */
 #define M16_ERR_CUDA 4          /* a CUDA runtime call failed */
 #define M16_ERR_TIMEOUT 5       /* a bounded device-side wait gave up */
-#define M16_ERR_TOO_LARGE 6     /* the request exceeds the fixed scratch of m16_maxflow_solve_static */
+#define M16_ERR_TOO_LARGE 6     /* the request exceeds a fixed capacity: the scratch of m16_maxflow_solve_static
+                                   or the work table of a server (max_work_items) */
 
 /* Longest Gaussian derivative kernel (taps = 2 * radius + 1) the Frangi entry points take. */
 #define M16_MAX_TAPS 127
@@ -163,9 +164,13 @@ int m16_maxflow_solve_ex(const float *img, const float *quat3, const double *sqe
  *
  * Limits: at most 262,144 voxels (e.g. 64 x 64 x 64) and at most 4,096
  * residual checks (num_iter / update + 2 <= 4096); larger requests return
- * M16_ERR_TOO_LARGE before any GPU work.  The first call on a device looks
- * the array's device address up (once per device, with that device current);
- * make that first call before any stream capture.  All calls share the one
+ * M16_ERR_TOO_LARGE before any GPU work.  Every call looks the array's
+ * device address up on the calling device, so the address stays right after
+ * a device reset.  With lazy module loading (the CUDA default) the array is
+ * reserved when the library's max-flow module first loads on a device --
+ * often this entry point's first call there -- and that call returns
+ * M16_ERR_CUDA if the device has no room left for it: make one warm-up call
+ * on each device before serving and before any stream capture.  All calls share the one
  * array: calls that overlap on the GPU (other streams, other host threads)
  * race and must be serialised by the caller.  The solve initialises every
  * scratch word it reads, so one call's leftovers never reach the next.

@@ -148,6 +148,11 @@ class BatchSteps(object):
             raise ValueError("invalid batch description")
         self._ws = N.workspace(nbytes)
         self._n = len(instances)
+        # every (non-capturing) stream the batch's work went to: end() orders
+        # itself after all of them, whichever stream is current then
+        self._streams = {}
+        self._last_stream = None
+        self._note_stream()
         h = ctypes.c_void_p()
         N.check("m16_batch_begin", L.m16_batch_begin(self._vd, len(volumes), self._idesc, self._n,
                                                      ctypes.byref(self._cp), N.ptr(self._ws), self._ws.numel(),
@@ -156,14 +161,29 @@ class BatchSteps(object):
         self.iterations = None
         self.residuals = None
 
+    def _note_stream(self):
+        torch = N.torch_mod()
+        if torch.cuda.is_current_stream_capturing():
+            return   # captured work runs wherever the graph is replayed, which the caller orders
+        s = torch.cuda.current_stream()
+        self._streams[s.cuda_stream] = s
+        self._last_stream = s
+
     def iterate(self, count):
+        """Enqueue count iterations on the current stream (capturable)."""
+        self._note_stream()
         N.check("m16_batch_iterate", self._L.m16_batch_iterate(self._h, int(count), N.stream_ptr()))
 
     def end(self):
         """u of every instance (CUDA tensors, instance order); sets
-        .iterations and .residuals."""
+        .iterations and .residuals.  Runs on the current stream after the
+        work that begin() and iterate() enqueued on any other stream."""
         if self._h is None:
             raise RuntimeError("the batch has ended")
+        cur = N.torch_mod().cuda.current_stream()
+        for s in self._streams.values():
+            if s.cuda_stream != cur.cuda_stream:
+                cur.wait_stream(s)
         its = (ctypes.c_int32 * self._n)()
         res = (ctypes.c_double * self._n)()
         h, self._h = self._h, None
@@ -174,11 +194,16 @@ class BatchSteps(object):
 
     def __del__(self):
         # a batch dropped without end(): finish it (m16_batch_end waits for
-        # its work) before the workspace goes back to the allocator
+        # its work) before the workspace goes back to the allocator.  It runs
+        # on the last stream the batch used, after the others' work.
         try:
             if getattr(self, "_h", None) is not None:
                 h, self._h = self._h, None
-                self._L.m16_batch_end(h, None, None, N.stream_ptr())
+                last = self._last_stream
+                for s in self._streams.values():
+                    if s.cuda_stream != last.cuda_stream:
+                        last.wait_stream(s)
+                self._L.m16_batch_end(h, None, None, ctypes.c_void_p(last.cuda_stream))
         except Exception:
             pass
 

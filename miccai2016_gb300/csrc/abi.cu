@@ -10,7 +10,7 @@ extern "C" const char *m16_status_string(int status)
     case M16_ERR_WORKSPACE: return "workspace missing, misaligned or too small";
     case M16_ERR_CUDA: return "CUDA runtime error";
     case M16_ERR_TIMEOUT: return "device-side wait timed out";
-    case M16_ERR_TOO_LARGE: return "request exceeds the fixed scratch of the no-allocation entry point";
+    case M16_ERR_TOO_LARGE: return "request exceeds a fixed capacity (the no-allocation entry point's scratch or a server's work table)";
     default: return "unknown status";
     }
 }

@@ -23,7 +23,6 @@
 #include <algorithm>
 #include <atomic>
 #include <memory>
-#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -737,8 +736,6 @@ constexpr int kStaticMaxChecks = 4096;
 // each region rounded up to 256 B
 constexpr size_t kStaticBytes = 11u << 20;   // 11 MiB >= 10,521,344 B needed at the limits
 
-std::mutex g_static_mu;
-void *g_static_scratch[64] = {};
 }  // namespace
 }  // namespace m16
 
@@ -746,20 +743,17 @@ static __device__ __align__(256) unsigned char m16_static_scratch[m16::kStaticBy
 
 namespace m16 {
 namespace {
-// Device address of the scratch array on the current device.  The first call
-// on a device resolves it with cudaGetSymbolAddress (host code cannot use the
-// array's name as a device address) and caches it per device.
+// Device address of the scratch array on the current device.  Host code cannot
+// use the array's name as a device address, so every call asks the runtime for
+// it, with the calling device current.  The lookup is cheap once the module is
+// loaded, and it is never stale: a device reset, or any teardown and
+// re-creation of the context, reloads the module and may move the array, and
+// the next lookup returns the new address.
 int static_scratch_on_current_device(void **out)
 {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return M16_ERR_CUDA;
-    std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_scratch[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, m16_static_scratch) != cudaSuccess || !p) return M16_ERR_CUDA;
-        g_static_scratch[dev] = p;
-    }
-    *out = g_static_scratch[dev];
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, m16_static_scratch) != cudaSuccess || !p) return M16_ERR_CUDA;
+    *out = p;
     return M16_OK;
 }
 }  // namespace

@@ -53,10 +53,30 @@ def stable_mst(points, voxel_size):
     return csr_matrix(minimum_spanning_tree(squareform(rank), overwrite=True))
 
 
+# above this many ridge points the dense R x R matrix of stable_mst is too
+# large, and prim_mst computes the same tree
+DENSE_MST_MAX_POINTS = 3000
+
+
+def prim_mst(points, voxel_size):
+    """The tree of stable_mst without the R x R matrix: Prim's algorithm under
+    the total order (distance, min(i, j), max(i, j)) of the edges, which is
+    the order stable_mst ranks them in.  Under a strict total order the
+    minimum spanning tree is unique, so Prim's and Kruskal's give the same
+    edge set.  The distances are pdist's: the square root of the summed
+    squared coordinate differences of the scaled points, in float64.
+    Returns the tree as a CSR matrix (one entry per edge)."""
+    pts = np.multiply(np.asarray(points, np.float64), voxel_size).reshape(-1, 3)
+    n = len(pts)
+    rows, cols = O.prim_mst_edges(pts)
+    return csr_matrix((np.ones(len(rows)), (rows, cols)), shape=(n, n))
+
+
 def adjust_ridge_directions(labeled_ridge, main_dirs, voxel_size):
-    """adjust_directions.py:365-417 (with the stable tree of stable_mst)"""
+    """adjust_directions.py:365-417 (with the stable tree of stable_mst, or
+    the same tree from prim_mst for many points)"""
     i_ridge = list(zip(*np.where(labeled_ridge)))
-    mst = stable_mst(i_ridge, voxel_size)
+    mst = (stable_mst if len(i_ridge) <= DENSE_MST_MAX_POINTS else prim_mst)(i_ridge, voxel_size)
     adjusted = np.ones_like(i_ridge, dtype=np.float32) * np.float32(np.nan)
     adjusted[0] = main_dirs[i_ridge[0]]
     get_children = lambda i: np.r_[mst[i].nonzero()[1], mst[:, i].nonzero()[0]]
@@ -90,9 +110,11 @@ def clean_ridge(labeled_ridge, ridge_coords, ridge_dirs, voxel_size):
 
 
 def advanced_adjuster(qeigs, response, threshold=(0.01, 0.3), voxel_size=(1, 1, 1), ridge_detection_only=False,
-                      clean=True):
+                      clean=True, stages=None):
     """AdvancedAdjuster.execute (adjust_directions.py:213-256) on the CPU.
-    Returns (adjusted dirs or None, final ridge, unadjusted main dirs)."""
+    Returns (adjusted dirs or None, final ridge, unadjusted main dirs).  A
+    dict passed as `stages` receives the ridge after the hysteresis, before
+    the cleaning ("ridge_hysteresis")."""
     qeigs = np.require(qeigs, np.float32, ["C", "A"])
     response = np.require(response, np.float32, ["C", "A"])
     voxel_size = tuple(np.multiply(np.ones(3), voxel_size))
@@ -106,6 +128,8 @@ def advanced_adjuster(qeigs, response, threshold=(0.01, 0.3), voxel_size=(1, 1, 
     if hyst:
         sure = np.logical_and(ridge, response >= threshold[1])
         ridge[:] = hysteresis_threshold(ridge, sure)
+    if stages is not None:
+        stages["ridge_hysteresis"] = ridge.copy()
     adjusted = None
     main = None
     if (not ridge_detection_only) or clean:

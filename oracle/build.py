@@ -23,8 +23,10 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
-REF_ROOT = os.environ.get("MICCAI2016_REFERENCE", "/root/reference")
-ORACLE_SOURCES = ["maxflow.c", "gvf.c", "frangi.c", "directions.c", "pipeline.c"]
+# the reference checkout: $MICCAI2016_REFERENCE, else a "reference" directory
+# beside this repository's root
+REF_ROOT = os.environ.get("MICCAI2016_REFERENCE") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
+ORACLE_SOURCES = ["maxflow.c", "gvf.c", "frangi.c", "directions.c"]
 
 CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-std=gnu11", "-Wall",
           "-Wno-unused-function", "-Wno-unknown-pragmas"]

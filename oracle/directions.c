@@ -127,3 +127,43 @@ void oracle_adjust_nonridge_signs(int64_t d0, int64_t d1, int64_t d2, float *dir
                 }
             }
 }
+
+/* The minimum spanning tree of the scaled ridge points (pts: n x 3 float64)
+ * that the reference takes from SciPy over squareform(pdist(...))
+ * (adjust_directions.py:376-379), with equal distances in (i, j) order: Prim's
+ * algorithm under the strict total order (distance, min(i, j), max(i, j)),
+ * whose tree is unique and equal to the stable Kruskal's.  Distances are
+ * pdist's: sqrt of the squared differences summed in axis order.  Writes the
+ * n - 1 edges as (lo[k], hi[k]), lo < hi, in the order Prim adds them.  O(n^2)
+ * time, O(n) memory. */
+void oracle_prim_mst(const double *pts, int64_t n, int64_t *lo_out, int64_t *hi_out)
+{
+    if (n < 2) return;
+    double *best_w = malloc(sizeof(double) * n);
+    int64_t *best_lo = malloc(sizeof(int64_t) * n), *best_hi = malloc(sizeof(int64_t) * n);
+    char *in_tree = calloc(n, 1);
+    for (int64_t j = 0; j < n; ++j) { best_w[j] = INFINITY; best_lo[j] = n; best_hi[j] = n; }
+    int64_t cur = 0;
+    for (int64_t k = 0; k < n - 1; ++k) {
+        in_tree[cur] = 1;
+        const double c0 = pts[3 * cur], c1 = pts[3 * cur + 1], c2 = pts[3 * cur + 2];
+        int64_t nxt = -1;
+        for (int64_t j = 0; j < n; ++j) {
+            if (in_tree[j]) continue;
+            const double e0 = pts[3 * j] - c0, e1 = pts[3 * j + 1] - c1, e2 = pts[3 * j + 2] - c2;
+            const double d = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+            const int64_t lo = j < cur ? j : cur, hi = j < cur ? cur : j;
+            if (d < best_w[j] || (d == best_w[j] && (lo < best_lo[j] || (lo == best_lo[j] && hi < best_hi[j])))) {
+                best_w[j] = d; best_lo[j] = lo; best_hi[j] = hi;
+            }
+            if (nxt < 0 || best_w[j] < best_w[nxt] ||
+                (best_w[j] == best_w[nxt] &&
+                 (best_lo[j] < best_lo[nxt] || (best_lo[j] == best_lo[nxt] && best_hi[j] < best_hi[nxt]))))
+                nxt = j;
+        }
+        lo_out[k] = best_lo[nxt];
+        hi_out[k] = best_hi[nxt];
+        cur = nxt;
+    }
+    free(best_w); free(best_lo); free(best_hi); free(in_tree);
+}

@@ -97,6 +97,8 @@ def _declare_oracle(L):
     L.oracle_complete_transformations.argtypes = [_i64, _vp, _vp]
     L.oracle_adjust_nonridge_signs.restype = None
     L.oracle_adjust_nonridge_signs.argtypes = [_i64, _i64, _i64, _vp, _vp, _vp, _i64, _vp]
+    L.oracle_prim_mst.restype = None
+    L.oracle_prim_mst.argtypes = [_vp, _i64, _vp, _vp]
     L.oracle_gvf_time_step.restype = ctypes.c_double
     L.oracle_gvf_time_step.argtypes = [_vp, ctypes.c_double, ctypes.c_int]
     L.oracle_gvf_run.restype = ctypes.c_int
@@ -517,3 +519,14 @@ def ref_adjust_nonridge_signs(dirs3, coords, rdirs, scaling=(1, 1, 1)):
     ref().ref_adjust_nonridge_signs(d.shape[0], d.shape[1], d.shape[2], _ptr(d), _ptr(ci), _ptr(di), _ptr(sc),
                                     len(coords))
     return d
+
+
+def prim_mst_edges(points_scaled):
+    """oracle_prim_mst: the (lo, hi) edges of the stable minimum spanning tree
+    of float64 points (n x 3, already scaled by the voxel size)."""
+    pts = np.require(points_scaled, dtype=np.float64, requirements=["C", "A"])
+    n = len(pts)
+    lo = np.zeros(max(n - 1, 0), np.int64)
+    hi = np.zeros(max(n - 1, 0), np.int64)
+    lib().oracle_prim_mst(_ptr(pts), n, _ptr(lo), _ptr(hi))
+    return lo, hi

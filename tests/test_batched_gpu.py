@@ -234,3 +234,46 @@ def test_steps_replayed_from_a_cuda_graph():
     assert np.all(steps.iterations == 120)
     for u, r in zip(us, ref):
         assert np.array_equal(u.view(np.uint32), r.view(np.uint32))
+
+
+def _oracle(v, inst, num_iter, update, error_bound):
+    from miccai2016_gb300 import phantom as P
+    from oracle import oracle as O
+    alpha = inst.get("alpha")
+    if alpha is None:
+        alpha = P.nonterminal_weights(v["grad2_f64"], inst["weighting"], inst["decay"]).astype(np.float32)
+    u, it, _ = O.maxflow_solve(v["img"], v["quats"], inst["eigs"], alpha, v["cs"], v["ct"], num_iter=num_iter,
+                               update=update, error_bound=error_bound)
+    return u, it
+
+
+def test_batch_instances_match_the_oracle():
+    """Each instance of a mixed batch (four-lane groups, a one-lane group, a
+    per-voxel alpha, ATV and TV, two volumes) against the CPU oracle
+    directly, not only through the plain CUDA path."""
+    vols = [_volume(21, (24, 28, 32)), _volume(22, (16, 20, 12))]
+    insts = [dict(volume=0, weighting=w, decay=d, eigs=e) for w, d in ((0.05, 30.0), (0.3, 1.0)) for e in (ATV, TV)]
+    insts += [dict(volume=0, weighting=0.01, decay=100.0, eigs=ATV),
+              dict(volume=1, weighting=0.1, decay=3.0, eigs=(1.0, 0.5, 0.25)),
+              dict(volume=1, alpha=np.full((16, 20, 12), 0.07, np.float32), eigs=TV)]
+    us, its = _batch(vols, insts, 90, 30, -1.0)
+    for k, inst in enumerate(insts):
+        u, it = _oracle(vols[inst["volume"]], inst, 90, 30, -1.0)
+        assert its[k] == it == 90
+        assert np.max(np.abs(us[k] - u)) <= U_TOL, k
+
+
+def test_batch_stopping_matches_the_oracle():
+    """Instances that stop at their own residual check stop where the oracle
+    stops (or one check away when the residual sits at the threshold)."""
+    vols = [_volume(23, (20, 24, 28))]
+    insts = [dict(volume=0, weighting=w, decay=d, eigs=ATV) for w in (0.01, 0.2) for d in (1.0, 30.0)]
+    us, its = _batch(vols, insts, 1500, 10, 2e-3)
+    same = 0
+    for k, inst in enumerate(insts):
+        u, it = _oracle(vols[0], inst, 1500, 10, 2e-3)
+        assert abs(int(its[k]) - it) <= 10
+        if int(its[k]) == it:
+            same += 1
+            assert np.max(np.abs(us[k] - u)) <= U_TOL, k
+    assert same >= len(insts) - 1

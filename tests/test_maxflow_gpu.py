@@ -116,6 +116,23 @@ def test_helix_64_fixed_iterations_parity(eigs_name, path):
         assert P.fast_dice(u, truth) > 0.3
 
 
+def test_helix_256_against_the_oracle():
+    """The 256^3 configuration (tube 12, helix 64, pitch 80, noise 1.0) for
+    20 fixed iterations against the oracle, plus the first residual checks
+    (update 10) -- the size the headline solve runs at."""
+    from miccai2016_gb300 import phantom as P
+    cfg = P.CONFIG_PLAIN_256
+    noisy, truth, quats, ntw, fgw, bgw = _helix_inputs(cfg)
+    kw = dict(num_iter=20, update=10, error_bound=-1.0)
+    c = _cutter(**kw)
+    u = c.execute(noisy, quats, P.ATV_EIGS, ntw, fgw, bgw, verbose=False)
+    ru, riters, rres = O.maxflow_solve(noisy, quats, P.ATV_EIGS, ntw, fgw, bgw, **kw)
+    assert c.last_iterations == riters == 20
+    assert np.max(np.abs(u - ru)) <= U_TOL
+    assert np.mean((u >= 0.5) != (ru >= 0.5)) <= MASK_FRAC
+    np.testing.assert_allclose(c.last_residuals, rres, rtol=1e-4)
+
+
 @pytest.mark.parametrize("path", PATHS)
 def test_residual_stop_matches_oracle(path):
     from miccai2016_gb300 import phantom as P

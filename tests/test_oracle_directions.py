@@ -197,3 +197,16 @@ def test_cleaning_of_a_ridge_without_background_drops_label_one_like_the_referen
         k1 = A.clean_ridge(ridge, c, d, (1.0, 1.0, 1.0))
         k2 = obj._do_clean_ridge(ridge, c, d)
     assert np.array_equal(k1, k2) and not k2.any()
+
+
+@pytest.mark.parametrize("n,voxel_size", [(300, (1, 1, 1)), (900, (1, 1, 1)), (600, (1.5, 0.7, 2.0)), (1, (1, 1, 1))])
+def test_prim_mst_is_the_stable_kruskal_tree(n, voxel_size):
+    """The oracle's O(R) memory tree (Prim under the (distance, i, j) order)
+    equals the dense stable Kruskal tree on lattice points full of ties."""
+    from oracle import adjust as A
+    rng = np.random.RandomState(n)
+    pts = sorted(set(tuple(p) for p in rng.randint(0, 11, (n, 3))))
+    a, b = A.stable_mst(pts, voxel_size), A.prim_mst(pts, voxel_size)
+    ea = set(tuple(sorted(e)) for e in zip(*a.nonzero()))
+    eb = set(tuple(sorted(e)) for e in zip(*b.nonzero()))
+    assert len(eb) == len(pts) - 1 and ea == eb

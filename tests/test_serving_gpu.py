@@ -156,3 +156,21 @@ def test_telemetry_counts_the_iterations_that_ran():
     assert info["voxel_iterations"] == want
     assert info["gpu_ms"] > 0.0
     srv.close()
+
+
+def test_served_results_match_the_oracle():
+    """Served requests (admitted at different times, fixed iteration count)
+    against the CPU oracle directly, not only through the plain CUDA path."""
+    from miccai2016_gb300 import phantom as P
+    from miccai2016_gb300.serving import ATV_EIGS
+    from oracle import oracle as O
+    pls = _payloads()
+    reqs = REQS[:4]
+    out = _serve(pls, reqs, stagger=2, num_iter=120, error_bound=-1.0)
+    for tag, (pi, w, d) in enumerate(reqs):
+        p = pls[pi]
+        alpha = P.nonterminal_weights(p["grad2"].numpy().astype(np.float64), w, d).astype(np.float32)
+        u, it, _ = O.maxflow_solve(p["img"].numpy(), p["quats"].numpy(), ATV_EIGS, alpha, p["cs"].numpy(),
+                                   p["ct"].numpy(), num_iter=120, update=30, error_bound=-1.0)
+        assert out[tag]["iterations"] == it == 120
+        assert np.max(np.abs(out[tag]["u"].numpy() - u)) <= U_TOL, tag

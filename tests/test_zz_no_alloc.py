@@ -5,10 +5,14 @@ not allocate while serving).  It keeps its scratch in a fixed array inside
 the library instead of a caller workspace.
 
 Called through the C ABI and checked against m16_maxflow_solve (the
-workspace entry point) on two calls in a row -- the second with a different
-shape and eigenvalue mode, so leftovers of the first call would show -- plus
-the size limit.  Collected last on purpose: if it fails, a run that stops at
-the first failure has already run every other test."""
+workspace entry point) on calls in a row -- the second with a different
+shape and eigenvalue mode, so leftovers of the first call would show.  Both
+entry points run the same two-sweep iteration on the same kernels, so u, the
+iteration count and every residual must agree bit for bit; each result is
+also checked against the CPU oracle within the max-flow tolerance.  After a
+warm-up call, a static call must leave the device's free memory unchanged.
+Collected last on purpose: if it fails, a run that stops at the first
+failure has already run every other test."""
 import ctypes
 import os
 import sys
@@ -23,9 +27,10 @@ import inputs as I  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
-U_TOL = 1e-3          # the tolerance of the max-flow parity tests
+U_TOL = 1e-3          # the tolerance of the max-flow parity tests against the oracle
 MAX_VOXELS = 262144   # the documented limit (64 x 64 x 64)
 TOO_LARGE = 6         # M16_ERR_TOO_LARGE
+CONST_SQ = (1.0, 10 ** -0.75, 10 ** -0.75)
 
 
 def _lib():
@@ -49,6 +54,8 @@ def _case(seed, shape, pointwise, supervised):
 
 
 def _solve(N, L, static, case, num_iter=60, update=10):
+    """One solve through the C ABI.  Returns (u, iterations, residuals, the
+    device's free bytes before and after the call)."""
     import torch
     img, q, alpha, cs, ct, sqe, lab = case
     shape = img.shape
@@ -56,7 +63,7 @@ def _solve(N, L, static, case, num_iter=60, update=10):
     dimg, dq, dal, dcs, dct, dsq, dlab = map(d, (img, q, alpha, cs, ct, sqe, lab))
     u = torch.empty(shape, dtype=torch.float32, device="cuda")
     cp = N.CutParams(0.2, 0.11, -1.0, num_iter, update, (ctypes.c_double * 3)(1, 1, 1))
-    sq = None if sqe is not None else (ctypes.c_double * 3)(1.0, 10 ** -0.75, 10 ** -0.75)
+    sq = None if sqe is not None else (ctypes.c_double * 3)(*CONST_SQ)
     it = ctypes.c_int32(0)
     cap = num_iter // update + 2
     res = (ctypes.c_double * cap)()
@@ -66,29 +73,54 @@ def _solve(N, L, static, case, num_iter=60, update=10):
               ctypes.byref(nres))
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     if static:
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         st = L.m16_maxflow_solve_static(*common, stream)
+        torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info()[0]
     else:
         nbytes = L.m16_maxflow_workspace_bytes(shape[0], shape[1], shape[2], ctypes.byref(cp))
         ws = N.workspace(nbytes)
         st = L.m16_maxflow_solve(*common, N.ptr(ws), ws.numel(), stream)
+        free_before = free_after = None
     assert st == 0, N.status_string(st)
     torch.cuda.synchronize()
-    return u.cpu().numpy(), it.value, np.array(res[:nres.value])
+    return u.cpu().numpy(), it.value, np.array(res[:nres.value]), free_before, free_after
+
+
+def _oracle(case, num_iter=60, update=10):
+    from oracle import oracle as O
+    img, q, alpha, cs, ct, sqe, lab = case
+    # the oracle takes eigenvalues and squares back: sqrt(float64(s)^2) == s exactly
+    eigs = np.square(sqe.astype(np.float64)) if sqe is not None else np.square(np.array(CONST_SQ))
+    u, iters, _ = O.maxflow_solve(img, q, eigs, alpha, cs, ct, labels=lab, num_iter=num_iter, update=update,
+                                  error_bound=-1.0)
+    return u, iters
 
 
 def test_static_matches_workspace_entry_point_on_two_calls_in_a_row():
     N, L = _lib()
     cases = [_case(1, (64, 64, 64), pointwise=False, supervised=False),   # the size limit exactly
              _case(2, (17, 9, 33), pointwise=True, supervised=True)]
+    first = None
     for case in cases:
-        u_s, it_s, r_s = _solve(N, L, True, case)
-        u_w, it_w, r_w = _solve(N, L, False, case)
+        u_s, it_s, r_s, _, _ = _solve(N, L, True, case)
+        u_w, it_w, r_w, _, _ = _solve(N, L, False, case)
         assert it_s == it_w == 60
-        assert np.max(np.abs(u_s - u_w)) <= U_TOL
-        # the static entry point runs the two-sweep iteration, the workspace
-        # one the fused kernel: the same per-voxel arithmetic, but the float
-        # sums of |err| are taken in a different order (columns vs tiles)
-        np.testing.assert_allclose(r_s, r_w, rtol=1e-4)
+        # the same two-sweep kernels on the same inputs: identical bits
+        assert np.array_equal(u_s, u_w)
+        assert np.array_equal(r_s, r_w)
+        u_o, it_o = _oracle(case)
+        assert it_o == 60
+        assert np.max(np.abs(u_s - u_o)) <= U_TOL
+        if first is None:
+            first = u_s
+    # a third call on the first case, after the second case left its state in
+    # the shared array: the same bits as the first call, and (every kernel and
+    # the array already loaded) no change in the device's free memory
+    u_s, it_s, _, free_before, free_after = _solve(N, L, True, cases[0])
+    assert it_s == 60 and np.array_equal(u_s, first)
+    assert free_after == free_before, (free_before, free_after)
 
 
 def test_static_rejects_requests_beyond_its_scratch():
