@@ -169,10 +169,11 @@ def _cpu_threads():
     return _HOST_THREADS
 
 
-def cpu_baseline(cfg, inp, iters=3):
+def cpu_baseline(cfg, inp, iters=30):
     """The reference kernels (oracle/_ref, when built here) or the oracle port
-    on the host cores: `iters` iterations of the solve, extrapolated to the
-    workload's iteration count.  Returns (solves/s, kind, seconds, sample)."""
+    on the host cores: `iters` iterations of the solve, timed, and the
+    workload's solves/s that rate gives.  Returns (solves/s, kind, seconds,
+    sample)."""
     os.environ.setdefault("OMP_NUM_THREADS", str(_cpu_threads()))
     os.environ.setdefault("OMP_PROC_BIND", "close")
     from oracle import oracle as O
@@ -185,34 +186,65 @@ def cpu_baseline(cfg, inp, iters=3):
     dt = time.perf_counter() - t0
     per_iter = dt / iters
     solves = 1.0 / (per_iter * cfg["num_iter"])
-    sample = "%d of the %d iterations of one %s solve, extrapolated linearly" % (
-        iters, cfg["num_iter"], "x".join(map(str, cfg["shape"])))
+    sample = "%d of the %d iterations of one %s solve, timed (%.2f s); solves/s = %d / (%d x that time)" % (
+        iters, cfg["num_iter"], "x".join(map(str, cfg["shape"])), dt, iters, cfg["num_iter"])
     return solves, kind, dt, sample
 
 
+def cpu_whole_solves(count=5):
+    """Whole solves of the 64^3 helix workload (300 fixed iterations) with the
+    reference kernels or the port on the host cores, timed end to end.
+    Returns (solves/s, kind, seconds per solve)."""
+    os.environ.setdefault("OMP_NUM_THREADS", str(_cpu_threads()))
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    from oracle import oracle as O
+    from miccai2016_gb300 import phantom as P
+    cfg = P.CONFIG_PLAIN_64
+    inp = _inputs(cfg)
+    kind = "reference" if O.ref() is not None else "port"
+    fn = O.ref_maxflow_solve if kind == "reference" else O.maxflow_solve
+    args = (inp["img"], inp["quats"], P.ATV_EIGS, inp["alpha"], inp["cs"], inp["ct"])
+    fn(*args, num_iter=cfg["num_iter"], update=30, error_bound=-1.0)   # warm-up
+    t0 = time.perf_counter()
+    for _ in range(count):
+        fn(*args, num_iter=cfg["num_iter"], update=30, error_bound=-1.0)
+    dt = (time.perf_counter() - t0) / count
+    return 1.0 / dt, kind, dt
+
+
 def run_reference(args, cfg):
+    """The reference's CPU path on the host cores.  Each step runs
+    --ref-iters iterations of the workload's solve and is timed as it runs;
+    ms_per_step is that observed time, and solves/s follows from the
+    iteration rate.  Whole 64^3 x 300-iteration solves are timed beside it."""
     rank, world, _ = _rank_info()
     if rank != 0:
         return
     inp = _inputs(cfg)
     for _ in range(args.warmup):
-        cpu_baseline(cfg, inp, iters=1)
-    vals = []
+        cpu_baseline(cfg, inp, iters=args.ref_iters)
+    vals, secs = [], []
     kinds = set()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         v, kind, dt, sample = cpu_baseline(cfg, inp, iters=args.ref_iters)
         vals.append(v)
+        secs.append(dt)
         kinds.add(kind)
     total = time.perf_counter() - t0
-    value = float(np.mean(vals))
+    value = args.ref_iters * len(secs) / (float(np.sum(secs)) * cfg["num_iter"])
+    whole_v, whole_kind, whole_s = cpu_whole_solves()
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(secs)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": _config(cfg),
+            "step": "%d of the workload's %d iterations, timed; value = iterations per second / %d" % (
+                args.ref_iters, cfg["num_iter"], cfg["num_iter"]),
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": _cpu_threads(), "kind": kinds.pop(),
                              "sample": sample},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "whole_solves_64cube_300it": {"solves_per_s": whole_v, "s_per_solve": whole_s, "kind": whole_kind,
+                                          "cores": _cpu_threads()},
             "wall_s": total}
     print(json.dumps(line), flush=True)
 
@@ -371,7 +403,8 @@ def run_ours(args, cfg):
                                       "bytes_per_voxel": F_BYTES},
                "fused_path": {"mf_fused_kernel_avg_ms": f_avg, "launches": fused_n, "GB/s": f_gbs,
                               "frac": f_gbs / peak, "bytes_per_voxel": F_BYTES}}
-    cpu_v, kind, cpu_dt, sample = cpu_baseline(cfg, inp, iters=args.ref_iters)
+    cpu_v, kind, cpu_dt, sample = cpu_baseline(cfg, inp, iters=args.cpu_iters) if rank == 0 else (
+        None, None, None, None)
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (analytic helix phantom, seeded noise)",
@@ -383,21 +416,67 @@ def run_ours(args, cfg):
                              "sample": sample},
             "clocks": clocks, "dice_fast": dice,
             "voxel_iterations_per_s": value * n * cfg["num_iter"]}
-    if cfg["name"] == "plain256" and not args.no_batched:   # the default workload also reports the grid search and serving
+    if cfg["name"] == "plain256" and not args.no_batched and world == 1:
+        # the default workload at N = 1 also reports the grid search, the ragged batch and serving, each
+        # against the plain one-solve-per-call path on the same instances (single-GPU measurements: a
+        # multi-GPU run reports the replicated solve only)
         line["batched"] = run_batched_grid()
+        line["ragged"] = ragged_batch(args.ragged_step)
         if args.served_requests > 0:
-            from miccai2016_gb300.serving import served_vs_plain
-            line["served"] = served_vs_plain(n_requests=args.served_requests, rate=50.0, pool=8,
-                                             max_resident=args.served_max_resident or None)
+            from miccai2016_gb300.serving import make_payloads, served_vs_plain
+            payloads = make_payloads(pool=args.served_pool)
+            line["served"] = served_vs_plain(n_requests=args.served_requests, rate=50.0, payloads=payloads,
+                                             max_resident=args.served_max_resident or None, check=args.served_check)
+            if args.served_saturated > 0:
+                line["served"]["saturated"] = served_vs_plain(n_requests=args.served_saturated, rate=None,
+                                                              payloads=payloads, seed=1, check=8)
+            del payloads
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
 
 
-def run_batched_grid(plain_sample=17):
-    """The batched grid search (one m16_batch_solve over all 425 ATV
-    instances of a 128^3 volume, each stopping at residual 1e-4) against the
-    plain one-solve-per-call path on a sample of the same instances."""
+def _plain_solves(cutter, vol, points, eigs):
+    """Every (weighting, decay) point solved one call at a time with
+    CmfCutQAnisotropicGpu.execute() on the device-resident volume; alpha =
+    w * exp(-|grad I|^2 / decay^2) is computed per call in float32, as the
+    batched flow sweep evaluates it.  Returns (u list, iterations, seconds)."""
+    import torch
+    from miccai2016_gb300 import phantom as P
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    us, its = [], []
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for (w, d) in points:
+        a = torch.exp(vol["grad2"] * np.float32(-1.0 / d ** 2)) * np.float32(w)
+        us.append(cutter.execute(vol["img"], vol["quats"], eigs, a, vol["cs"], vol["ct"], verbose=False))
+        its.append(cutter.last_iterations)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return us, np.asarray(its, np.int64), e0.elapsed_time(e1) / 1000.0
+
+
+def _timed_batch(bc, vols, insts, **kw):
+    import torch
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    us = bc.solve(vols, insts, **kw)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return us, bc.last_iterations.copy(), e0.elapsed_time(e1) / 1000.0
+
+
+def run_batched_grid():
+    """The batched grid search of the 128^3 noise-1.5 helix: one
+    m16_batch_solve over all 425 ATV (weighting, decay) instances, each
+    stopping at residual 1e-4, against all 425 plain one-solve-per-call
+    solves of the same instances; then the reference experiment's full loop,
+    ATV and TV at every grid point (phantom_experiment.py:350-368), as one
+    batch of 850 against 850 plain solves.  Dice is compared instance by
+    instance."""
     import torch
     from miccai2016_gb300 import phantom as P, pipeline
     from miccai2016_gb300.batched import BatchedCut
@@ -417,88 +496,161 @@ def run_batched_grid(plain_sample=17):
     vol = bc.prepare_volume(noisy, cut["quats"], cut["fgw"], cut["bgw"], grad2=cut["grad2"])
     grid = [(w, d) for w in cfg["weightings"] for d in cfg["decays"]]
     insts = [dict(volume=0, weighting=w, decay=d, eigs=P.ATV_EIGS) for (w, d) in grid]
-    # warm-up: a two-instance batch loads the kernels
+    insts_tv = [dict(volume=0, weighting=w, decay=d, eigs=P.TV_EIGS) for (w, d) in grid]
+    truth_d = torch.from_numpy(truth).cuda()
+    n_vox = int(np.prod(cfg["shape"]))
+    cp = CmfCutQAnisotropicGpu.CutParameters()
+    cp.num_iter, cp.update, cp.error_bound = cfg["num_iter"], cfg["update"], cfg["error_bound"]
+    cutter = CmfCutQAnisotropicGpu(cp)
+    # warm-up: a two-instance batch and one plain solve load the kernels
     wp = BatchedCut.CutParameters()
     wp.num_iter, wp.update, wp.error_bound = 60, 30, -1.0
     BatchedCut(wp).solve([vol], insts[:2])
-    torch.cuda.synchronize()
-    stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    us = bc.solve([vol], insts)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    batched_s = e0.elapsed_time(e1) / 1000.0
-    iters = bc.last_iterations.copy()
+    _plain_solves(cutter, vol, grid[:1], P.ATV_EIGS)
+
+    # ---- the 425 ATV instances
+    us, iters, batched_s = _timed_batch(bc, [vol], insts)
     tuned_bps = bc.last_blocks_per_sm
-    truth_d = torch.from_numpy(truth).cuda()
     dice_b = np.asarray(fast_dice(us, truth_d))
-    # the experiment's Dice of the best instance: its largest 6-connected component
     best = int(np.argmax(dice_b))
     t_dl = time.perf_counter()
     best_dice_true = dice_largest(us[best], truth_d)
     dice_largest_s = time.perf_counter() - t_dl
     del us
-    # the same batch with the default tile shape and with direct launches
     variants = {}
     for name, kw in (("default_tile_shape", dict(tune=False)), ("no_graphs", dict(graphs=False))):
-        e0.record(stream)
-        vu = bc.solve([vol], insts, **kw)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        variants[name] = {"s": e0.elapsed_time(e1) / 1000.0, "blocks_per_sm": bc.last_blocks_per_sm,
-                          "same_iterations": bool(np.array_equal(bc.last_iterations, iters))}
+        vu, vit, vs = _timed_batch(bc, [vol], insts, **kw)
+        variants[name] = {"s": vs, "blocks_per_sm": bc.last_blocks_per_sm,
+                          "same_iterations": bool(np.array_equal(vit, iters))}
         del vu
-    # plain path on a sample: the decays of the best weighting (17 instances)
-    wi = best // len(cfg["decays"])
-    sample = [wi * len(cfg["decays"]) + k for k in range(len(cfg["decays"]))][:plain_sample]
-    cp = CmfCutQAnisotropicGpu.CutParameters()
-    cp.num_iter, cp.update, cp.error_bound = cfg["num_iter"], cfg["update"], cfg["error_bound"]
-    cutter = CmfCutQAnisotropicGpu(cp)
-    d_img, d_q = vol["img"], vol["quats"]
-    # alpha = w * exp(-|grad I|^2 / decay^2) in float32, as the batched flow sweep evaluates it
-    alphas = [(torch.exp(vol["grad2"] * np.float32(-1.0 / grid[k][1] ** 2)) * np.float32(grid[k][0])).contiguous()
-              for k in sample]
-    cutter.execute(d_img, d_q, P.ATV_EIGS, alphas[0], vol["cs"], vol["ct"], verbose=False)   # warm-up
-    torch.cuda.synchronize()
-    e0.record(stream)
-    plain_u = []
-    plain_iters = []
-    for k, a in zip(sample, alphas):
-        plain_u.append(cutter.execute(d_img, d_q, P.ATV_EIGS, a, vol["cs"], vol["ct"], verbose=False))
-        plain_iters.append(cutter.last_iterations)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    plain_s = e0.elapsed_time(e1) / 1000.0
+    plain_u, plain_iters, plain_s = _plain_solves(cutter, vol, grid, P.ATV_EIGS)
     dice_p = np.asarray(fast_dice(plain_u, truth_d))
-    plain_best_dice_true = dice_largest(plain_u[sample.index(best)], truth_d) if best in sample else None
-    n_vox = int(np.prod(cfg["shape"]))
-    vox_it = float(np.sum(iters)) * n_vox
-    batched_rate = len(insts) / batched_s
-    plain_rate = len(sample) / plain_s
-    return {"workload": "425-instance ATV grid search (25 weightings x 17 decays), 128x128x128 helix, "
-                        "noise sigma 1.5, stop at residual 1e-4 (update 30, at most 3000 iterations)",
-            "solves_per_s": batched_rate, "plain_solves_per_s": plain_rate,
-            "speedup_vs_plain": batched_rate / plain_rate,
-            "plain_sample": "the 17 decays of the best weighting, one CmfCutQAnisotropicGpu.execute() each",
-            "batched_s": batched_s, "plain_sample_s": plain_s,
-            "iterations": {"min": int(iters.min()), "median": float(np.median(iters)), "max": int(iters.max())},
-            "voxel_iterations_per_s": vox_it / batched_s,
-            "achieved_gbs_state": 60.0 * vox_it / batched_s / 1e9,   # flow 28 + label 32 B of state per voxel-iteration
-            "best_dice_fast": float(dice_b[best]), "best_weighting": grid[best][0], "best_decay": grid[best][1],
-            "best_dice_largest_component": best_dice_true, "plain_best_dice_largest_component": plain_best_dice_true,
-            "dice_largest_component_s": dice_largest_s,
-            "max_dice_diff_vs_plain": float(np.max(np.abs(dice_b[sample] - dice_p))),
-            "iteration_diff_vs_plain": int(np.max(np.abs(iters[sample] - np.asarray(plain_iters)))),
-            "tuned_blocks_per_sm": tuned_bps, "variants": variants,
-            "shared_preparation_s": prep_s, "preparation_stages_s": stages,
-            "ridge_points": cut["ridge_points"]}
+    plain_best_dice_true = dice_largest(plain_u[best], truth_d)
+    del plain_u
+    vox_it_b = float(np.sum(iters)) * n_vox
+    vox_it_p = float(np.sum(plain_iters)) * n_vox
+    atv = {"workload": "425-instance ATV grid search (25 weightings x 17 decays), 128x128x128 helix, "
+                       "noise sigma 1.5, stop at residual 1e-4 (update 30, at most 3000 iterations)",
+           "solves_per_s": len(insts) / batched_s, "plain_solves_per_s": len(insts) / plain_s,
+           "speedup_vs_plain": plain_s / batched_s,
+           "plain_sample": "all 425 instances, one CmfCutQAnisotropicGpu.execute() each",
+           "batched_s": batched_s, "plain_s": plain_s,
+           "iterations": {"min": int(iters.min()), "median": float(np.median(iters)), "max": int(iters.max())},
+           "voxel_iterations_per_s": vox_it_b / batched_s, "plain_voxel_iterations_per_s": vox_it_p / plain_s,
+           "speedup_voxel_iterations_per_s": (vox_it_b / batched_s) / (vox_it_p / plain_s),
+           "achieved_gbs_state": 60.0 * vox_it_b / batched_s / 1e9,   # 60 B of per-instance state per voxel-iteration
+           "best_dice_fast": float(dice_b[best]), "best_weighting": grid[best][0], "best_decay": grid[best][1],
+           "best_dice_largest_component": best_dice_true, "plain_best_dice_largest_component": plain_best_dice_true,
+           "dice_largest_component_s": dice_largest_s,
+           "max_dice_diff_vs_plain": float(np.max(np.abs(dice_b - dice_p))),
+           "iteration_diff_vs_plain": int(np.max(np.abs(iters - plain_iters))),
+           "tuned_blocks_per_sm": tuned_bps, "variants": variants,
+           "shared_preparation_s": prep_s, "preparation_stages_s": stages,
+           "ridge_points": cut["ridge_points"]}
+
+    # ---- ATV and TV at every grid point, as the reference experiment runs it
+    mixed = insts + insts_tv
+    us, iters2, batched2_s = _timed_batch(bc, [vol], mixed)
+    dice_b2 = np.asarray(fast_dice(us, truth_d))
+    del us
+    tv_u, tv_iters, tv_s = _plain_solves(cutter, vol, grid, P.TV_EIGS)
+    dice_tv = np.asarray(fast_dice(tv_u, truth_d))
+    del tv_u
+    plain2_s = plain_s + tv_s
+    plain2_iters = np.concatenate([plain_iters, tv_iters])
+    dice_p2 = np.concatenate([dice_p, dice_tv])
+    vox_it_b2 = float(np.sum(iters2)) * n_vox
+    vox_it_p2 = float(np.sum(plain2_iters)) * n_vox
+    n_atv = len(insts)
+    both = {"workload": "850 instances: ATV and TV at each of the 25 x 17 grid points (the reference experiment's "
+                        "loop), same volume and stopping rule",
+            "solves_per_s": len(mixed) / batched2_s, "plain_solves_per_s": len(mixed) / plain2_s,
+            "speedup_vs_plain": plain2_s / batched2_s, "batched_s": batched2_s, "plain_s": plain2_s,
+            "voxel_iterations_per_s": vox_it_b2 / batched2_s, "plain_voxel_iterations_per_s": vox_it_p2 / plain2_s,
+            "best_dice_fast_atv": float(dice_b2[:n_atv].max()), "best_dice_fast_tv": float(dice_b2[n_atv:].max()),
+            "max_dice_diff_vs_plain": float(np.max(np.abs(dice_b2 - dice_p2))),
+            "iteration_diff_vs_plain": int(np.max(np.abs(iters2 - plain2_iters)))}
+    atv["atv_and_tv"] = both
+    return atv
+
+
+def run_grid_quality(args):
+    """Where the grid search's Dice comes from: the 425-instance ATV grid on
+    the 128^3 noise-1.5 helix, batched, under each combination of
+      * the quaternions: the GPU pipeline's (Frangi, sign adjustment, GVF,
+        completion) or the analytic helix tangents;
+      * the pipeline's parameters: the workload's (Frangi sigma 2, 4, 6; GVF
+        mu 0.2, 100 iterations) or the reference experiment's
+        (phantom_experiment.py:228-236, 266-279: Frangi scales
+        (r_min / 1.2, r_max * 1.2, 16) for tube radii 3-6, GVF mu 10^0.5,
+        300 iterations);
+      * the stopping rule: residual 1e-4 (the workload's) or 1e-6 (the
+        reference experiment's cutter, phantom_experiment.py:248-256),
+        update 30, at most 3000 iterations.
+    Prints one JSON line with the best fast Dice, its (weighting, decay) and
+    the iteration counts of each combination."""
+    import torch
+    torch.cuda.set_device(0)
+    from miccai2016_gb300 import phantom as P, pipeline
+    from miccai2016_gb300.batched import BatchedCut
+    from miccai2016_gb300.capacities import fast_dice
+    from miccai2016_gb300.labeling import dice_largest
+    cfg = P.CONFIG_GRID_128
+    nearest = P.helix_nearest(cfg["shape"], cfg["tube_radius"], cfg["helix_radius"], cfg["pitch"])
+    noisy, truth = P.helix_phantom(cfg["shape"], cfg["tube_radius"], cfg["helix_radius"], cfg["pitch"],
+                                   cfg["sigma"], cfg["seed"], nearest=nearest)
+    analytic = P.squeeze_frames(P.helix_tangents(cfg["shape"], cfg["tube_radius"], cfg["helix_radius"],
+                                                 cfg["pitch"], nearest=nearest)).astype(np.float32)
+    truth_d = torch.from_numpy(truth).cuda()
+    preps = {"workload": dict(scales=cfg["scales"], gvf_mu=cfg["gvf_mu"], gvf_iterations=cfg["gvf_iter"]),
+             "reference_experiment": dict(scales=(3.0 / 1.2, 6.0 * 1.2, 16), gvf_mu=10 ** 0.5, gvf_iterations=300)}
+    grid = [(w, d) for w in cfg["weightings"] for d in cfg["decays"]]
+    insts = [dict(volume=0, weighting=w, decay=d, eigs=P.ATV_EIGS) for (w, d) in grid]
+    out = {}
+    cut0 = None
+    for pname, kw in preps.items():
+        t0 = time.perf_counter()
+        cut, _ = pipeline.prepare_cut_inputs(noisy, cfg["sigma"], **kw)
+        prep_s = time.perf_counter() - t0
+        cut0 = cut0 or cut
+        for qname, quats in (("pipeline", cut["quats"]), ("analytic", analytic)):
+            if qname == "analytic" and pname != "workload":
+                continue
+            for eb in (1e-4, 1e-6):
+                bp = BatchedCut.CutParameters()
+                bp.num_iter, bp.update, bp.error_bound = 3000, 30, eb
+                bc = BatchedCut(bp)
+                vol = bc.prepare_volume(noisy, quats, cut["fgw"], cut["bgw"], grad2=cut["grad2"])
+                t0 = time.perf_counter()
+                us = bc.solve([vol], insts)
+                torch.cuda.synchronize()
+                solve_s = time.perf_counter() - t0
+                dice = np.asarray(fast_dice(us, truth_d))
+                best = int(np.argmax(dice))
+                out["%s/%s/stop %g" % (qname, pname if qname == "pipeline" else "-", eb)] = {
+                    "best_dice_fast": float(dice[best]),
+                    "best_dice_largest_component": dice_largest(us[best], truth_d),
+                    "best_weighting": grid[best][0], "best_decay": grid[best][1],
+                    "iterations_median": float(np.median(bc.last_iterations)),
+                    "iterations_at_best": int(bc.last_iterations[best]),
+                    "batch_s": solve_s, "preparation_s": prep_s if qname == "pipeline" else None,
+                    "ridge_points": cut["ridge_points"] if qname == "pipeline" else None}
+                del us
+    print(json.dumps({"impl": "ours", "workload": "grid quality: 425 ATV instances, 128^3 helix, noise 1.5",
+                      "results": out}), flush=True)
 
 
 RAGGED_SHAPES = [(96, 96, 96), (128, 128, 192), (160, 160, 160), (224, 224, 160)]
 
 
 def run_ragged(args):
+    """--workload ragged: prints ragged_batch() as one JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps(dict(impl="ours", **ragged_batch(args.ragged_step))), flush=True)
+
+
+def ragged_batch(step=1):
     """Ragged batch: noise levels linspace(0.1, 1.5, 15)[::step] x the four
     volume shapes, each a helix phantom with its own helix radius (0.2-0.3 of
     the smallest extent) and tube radius (2-6 voxels) drawn from a seeded
@@ -507,14 +659,13 @@ def run_ragged(args):
     m16_batch_solve (ATV, weighting 10^-1.25, decay 10^1.5, stop at residual
     1e-4, update 30, at most 3000 iterations) against the same cuts solved one
     by one with CmfCutQAnisotropicGpu.execute() on device-resident inputs.
-    Prints one JSON line."""
+    Returns a dict."""
     import torch
-    torch.cuda.set_device(0)
     from miccai2016_gb300 import phantom as P, pipeline
     from miccai2016_gb300.batched import BatchedCut
     from miccai2016_gb300.capacities import fast_dice
     from miccai2016_gb300.continuous_cut_anisotropic_gpu import CmfCutQAnisotropicGpu
-    sigmas = np.linspace(0.1, 1.5, 15)[::max(1, args.ragged_step)]
+    sigmas = np.linspace(0.1, 1.5, 15)[::max(1, step)]
     rng = np.random.RandomState(2016)
     w, d = 10 ** -1.25, 10 ** 1.5
     vols, truths, prep = [], [], []
@@ -567,7 +718,7 @@ def run_ragged(args):
         dice_p.append(fast_dice(u, t))
     n = len(vols)
     vox = np.array([int(np.prod(v["shape"])) for v in vols], np.float64)
-    line = {"impl": "ours", "workload": "ragged batch: %d noise levels x shapes %s, helix phantoms, GPU pipeline "
+    return {"workload": "ragged batch: %d noise levels x shapes %s, helix phantoms, GPU pipeline "
                                         "per volume, ATV cut w=10^-1.25 decay=10^1.5, stop at residual 1e-4" % (
                                             len(sigmas), RAGGED_SHAPES),
             "volumes": n, "batched_solves_per_s": n / batched_s, "plain_solves_per_s": n / plain_s,
@@ -579,7 +730,6 @@ def run_ragged(args):
             "dice_fast": {"min": float(dice_b.min()), "median": float(np.median(dice_b)), "max": float(dice_b.max())},
             "preparation_s_per_volume": {"median": float(np.median(prep)), "max": float(np.max(prep))},
             "preparation_total_s": t_prep}
-    print(json.dumps(line), flush=True)
 
 
 STAGE_BYTES = {
@@ -701,6 +851,7 @@ def run_stages(args, cfg):
             main_dirs = adj._qeigs_to_main_dirs()
             coords, rdirs = adj._adjust_ridge_directions(adj.ridge, main_dirs)
         host_s = time.perf_counter() - t0
+        adj_timings = dict(adj.timings)
         R = int(len(coords))
         d_coords = torch.from_numpy(np.ascontiguousarray(coords, np.uint16).view(np.int16)).to(dev)
         d_rdirs = torch.from_numpy(np.ascontiguousarray(rdirs, np.float32)).to(dev)
@@ -711,7 +862,7 @@ def run_stages(args, cfg):
                                                            N.ptr(work), d0, d1, d2, N.ptr(d_coords), N.ptr(d_rdirs),
                                                            R, sc, N.ptr(nws), nws.numel(), sp)),
               n, "voxels", extra=lambda ms: {
-                  "ridge_points": R, "host_steps_s": host_s,
+                  "ridge_points": R, "host_steps_s": host_s, "host_steps_breakdown_s": adj_timings,
                   "host_steps": "hysteresis, ridge MST and sign propagation, cleaning (numpy/scipy)",
                   "kernel": "m16_adjust_nonridge_signs_indexed (cell index build + shell search)",
                   "brute_force_equivalent_evaluations_per_s": n * R / (ms * 1e-3)})
@@ -823,7 +974,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain256")
-    ap.add_argument("--ref-iters", type=int, default=3, help="iterations per CPU-baseline sample")
+    ap.add_argument("--ref-iters", type=int, default=30,
+                    help="iterations per step of the reference arm and per CPU-baseline sample")
     ap.add_argument("--stages", default="",
                     help="stages workloads: comma-separated subset of %s (default: all)" % ",".join(STAGES))
     ap.add_argument("--ragged-step", type=int, default=1,
@@ -832,8 +984,16 @@ def main():
                     help="skip the batched grid search and the serving comparison of the default workload")
     ap.add_argument("--served-max-resident", type=int, default=0,
                     help="serving comparison: at most this many requests resident at once (0: no limit)")
-    ap.add_argument("--served-requests", type=int, default=96,
-                    help="requests of the serving comparison (0 skips it)")
+    ap.add_argument("--served-requests", type=int, default=10000,
+                    help="requests of the serving comparison at 50 req/s (0 skips it)")
+    ap.add_argument("--served-pool", type=int, default=48,
+                    help="serving comparison: distinct helix volumes the requests draw from")
+    ap.add_argument("--served-check", type=int, default=32,
+                    help="serving comparison: requests whose u is compared between the two loops")
+    ap.add_argument("--served-saturated", type=int, default=500,
+                    help="serving comparison: requests of the saturated run (all at t = 0; 0 skips it)")
+    ap.add_argument("--cpu-iters", type=int, default=100,
+                    help="iterations of the CPU-baseline sample of the default arm")
     ap.add_argument("--paths", default="two_sweeps,fused,pairs",
                     help="paths workloads: which iteration paths to time")
     ap.add_argument("--pair-zc", default="",
@@ -844,6 +1004,9 @@ def main():
         return
     if args.workload == "ragged":
         run_ragged(args)
+        return
+    if args.workload == "grid_quality":
+        run_grid_quality(args)
         return
     if args.workload.startswith("stages"):
         run_stages(args, _workload("plain" + args.workload[len("stages"):]))

@@ -17,6 +17,7 @@ runs m16_complete_transformations.
 from __future__ import annotations
 
 import ctypes
+import time
 
 import numpy as np
 
@@ -137,11 +138,14 @@ class AdvancedAdjuster(TreePrintable):
         None when ridge_detection_only."""
         assert self.response.shape == self.qeigs.shape[:3] and self.qeigs.shape[3] == 3
         torch = N.torch_mod()
+        self.timings = {}   # seconds per step of the last execute()
         self._d_qeigs = N.to_device_f32(self.qeigs)
-        labeled_ridge = self._label_ridge()
+        with self._timed("ridge_candidates_and_hysteresis"):
+            labeled_ridge = self._label_ridge()
         adjusted = None
         if (not self.ridge_detection_only) or self.clean_ridge:
-            main_dirs = self._qeigs_to_main_dirs()
+            with self._timed("main_directions"):
+                main_dirs = self._qeigs_to_main_dirs()
             # before cleaning, only the per-segment norms matter (see _adjust_ridge_directions)
             ridge_coords, ridge_dirs = self._adjust_ridge_directions(labeled_ridge, main_dirs,
                                                                      join_components=not self.clean_ridge)
@@ -150,11 +154,27 @@ class AdvancedAdjuster(TreePrintable):
                 if not self.ridge_detection_only:
                     ridge_coords, ridge_dirs = self._adjust_ridge_directions(labeled_ridge, main_dirs)
             if not self.ridge_detection_only:
-                adjusted = self._adjust_all_directions(ridge_coords, ridge_dirs)
+                with self._timed("nearest_ridge_flip"):
+                    adjusted = self._adjust_all_directions(ridge_coords, ridge_dirs)
         del self._d_qeigs
         self._d_main = None
         torch.cuda.current_stream().synchronize()
         return adjusted
+
+    class _Timer(object):
+        def __init__(self, timings, name):
+            self.t, self.name = timings, name
+
+        def __enter__(self):
+            self.t0 = time.perf_counter()
+
+        def __exit__(self, *exc):
+            self.t[self.name] = self.t.get(self.name, 0.0) + time.perf_counter() - self.t0
+
+    def _timed(self, name):
+        if not hasattr(self, "timings"):
+            self.timings = {}
+        return AdvancedAdjuster._Timer(self.timings, name)
 
     def _label_ridge(self):
         """adjust_directions.py:258-288.  The ridge candidates and the main
@@ -182,7 +202,10 @@ class AdvancedAdjuster(TreePrintable):
         directions are longest (adjust_directions.py:290-339).  Per segment the
         directions are summed in the reference's order (C order of the voxels)."""
         scaled = ridge_dirs * self.__voxel_size   # float32 * tuple -> float64, as in the reference
-        components, n_lab = label26(labeled_ridge, where=self.labeler)
+        with self._timed("clean_labels"):
+            components, n_lab = label26(labeled_ridge, where=self.labeler)
+        t_sums = self._timed("clean_segment_sums")
+        t_sums.__enter__()
         # np.unique(components)[1:] without the sort: the labels are 1..n_lab,
         # and "[1:]" drops label 1 too when no voxel is background
         labels = np.arange(1 if len(ridge_coords) < components.size else 2, n_lab + 1)
@@ -196,6 +219,7 @@ class AdvancedAdjuster(TreePrintable):
             lengths[lab] = np.linalg.norm(np.sum(scaled[order[s:e]], axis=0))
         ordered = sorted(lengths, key=lambda k: lengths[k], reverse=True)
         boundary = int(np.ceil(3 * np.log(np.e + len(ordered))))
+        t_sums.__exit__()
         print("Keeping %s of %s labels." % (boundary, len(ordered)))
         kept = ordered[:boundary]
         keep = np.zeros(n_lab + 1, dtype=bool)   # np.in1d(components, kept) as a table lookup
@@ -228,12 +252,15 @@ class AdvancedAdjuster(TreePrintable):
         MST edges between groups of points more than one step apart, so each
         group keeps its own global sign; the cleaning only uses per-segment
         norms of sums, which that sign does not change."""
-        coords = np.argwhere(labeled_ridge)   # C order, as zip(*np.where(...))
+        with self._timed("ridge_coordinates"):
+            coords = np.argwhere(labeled_ridge)   # C order, as zip(*np.where(...))
         if len(coords) == 0:
             raise ValueError("no ridge points: nothing to propagate directions along")
-        a, b = ridge_mst_edges(coords, self.voxel_size, join_components=join_components, local=self.mst_local)
-        dirs = main_dirs[coords[:, 0], coords[:, 1], coords[:, 2]]
-        adjusted = propagate_signs(len(coords), a, b, dirs)
+        with self._timed("mst_local" if not join_components else "mst_local_and_joins"):
+            a, b = ridge_mst_edges(coords, self.voxel_size, join_components=join_components, local=self.mst_local)
+        with self._timed("sign_propagation"):
+            dirs = main_dirs[coords[:, 0], coords[:, 1], coords[:, 2]]
+            adjusted = propagate_signs(len(coords), a, b, dirs)
         return np.asarray(coords, dtype=np.uint16, order="C"), adjusted
 
     def _adjust_all_directions(self, ridge_coords, ridge_dirs):

@@ -6,8 +6,11 @@
 // These decide discrete outcomes (ridge or not, nearest ridge point, sign), so
 // their arithmetic follows the reference's rounding sequence: explicit _rn
 // intrinsics instead of contracted multiply-adds, and the quaternion
-// expansion's trigonometry in double rounded to float (the reference's
-// OpenCL C promotes `* 0.5` to double).
+// expansion's trigonometry as the float nearest to the exact value (the
+// reference's OpenCL C promotes `* 0.5` to double and rounds cos/sin to
+// float).  That float comes from a double-float evaluation in single
+// precision (ffsincos.cuh) and, where its error bound reaches a rounding
+// boundary or the argument lies outside [-4, 4], from double precision.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <float.h>
@@ -16,25 +19,36 @@
 #include <climits>
 
 #include "common.cuh"
+#include "ffsincos.cuh"
 
 namespace m16 {
 namespace {
 
 constexpr int kBX = 32, kBY = 8;
 
+// float(sin(xd)) and float(cos(xd)) of the double xd = x: single precision
+// where certain, double precision otherwise
+__device__ __forceinline__ void sincos_ref(float x, double xd, float *s, float *c)
+{
+    if (ff::sincos_rn(x, s, c)) return;
+    double sd, cd;
+    sincos(xd, &sd, &cd);
+    *s = (float)sd;
+    *c = (float)cd;
+}
+
 // qexpand with the reference's precision: half angles rounded to float, the
-// cosines and sines evaluated in double and rounded to float.
+// cosines and sines rounded to float from their exact values.  theta / 2 is
+// exact in float except for subnormal theta, where the rounded half still
+// gives the same floats (|x| < 2^-12: sin rounds to the rounded x, cos to 1).
 __device__ __forceinline__ void qexpand_ref(float phi, float theta, float psi, float q[4])
 {
     const float pp = __fmul_rn(__fadd_rn(phi, psi), 0.5f);
     const float pm = __fmul_rn(__fsub_rn(phi, psi), 0.5f);
-    double s, c;
-    sincos((double)theta * 0.5, &s, &c);
-    const float ct = (float)c, st = (float)s;
-    sincos((double)pp, &s, &c);
-    const float cpp = (float)c, spp = (float)s;
-    sincos((double)pm, &s, &c);
-    const float cpm = (float)c, spm = (float)s;
+    float ct, st, cpp, spp, cpm, spm;
+    sincos_ref(__fmul_rn(theta, 0.5f), (double)theta * 0.5, &st, &ct);
+    sincos_ref(pp, (double)pp, &spp, &cpp);
+    sincos_ref(pm, (double)pm, &spm, &cpm);
     q[0] = __fmul_rn(cpp, ct);
     q[1] = __fmul_rn(cpm, st);
     q[2] = __fmul_rn(spm, st);

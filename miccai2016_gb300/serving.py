@@ -202,12 +202,9 @@ GRID_DECAYS = np.logspace(-1, 3, 17)
 ATV_EIGS = (1.0, 10 ** -1.5, 10 ** -1.5)
 
 
-def make_workload(n_requests, rate=50.0, pool=16, side_range=(64, 320), sigma_range=(0.1, 1.5), seed=0):
-    """Poisson arrivals at `rate` per second; each request draws a volume from
-    a pool of `pool` helix volumes (sides uniform in side_range per axis,
-    noise sigma uniform in sigma_range) and a (weighting, decay) point of the
-    25 x 17 grid.  Returns (payloads, requests) with requests = list of dicts
-    (tag, arrival, payload index, weighting, decay)."""
+def make_payloads(pool=16, side_range=(64, 320), sigma_range=(0.1, 1.5), seed=0):
+    """`pool` helix volumes: sides uniform in side_range, drawn per axis
+    independently; noise sigma uniform in sigma_range."""
     rng = np.random.RandomState(seed)
     payloads = []
     for k in range(pool):
@@ -217,8 +214,25 @@ def make_workload(n_requests, rate=50.0, pool=16, side_range=(64, 320), sigma_ra
         p["sigma"] = sigma
         p["shape"] = shape
         payloads.append(p)
-    gaps = rng.exponential(1.0 / rate, size=n_requests)
-    arrivals = np.cumsum(gaps) - gaps[0]
+    return payloads
+
+
+def make_workload(n_requests, rate=50.0, pool=16, side_range=(64, 320), sigma_range=(0.1, 1.5), seed=0,
+                  payloads=None):
+    """Poisson arrivals at `rate` per second (rate None: all at t = 0); each
+    request draws a volume from a pool of `pool` helix volumes (make_payloads,
+    or the given payloads) and a (weighting, decay) point of the 25 x 17
+    grid.  Returns (payloads, requests) with requests = list of dicts (tag,
+    arrival, payload index, weighting, decay)."""
+    if payloads is None:
+        payloads = make_payloads(pool, side_range, sigma_range, seed)
+    pool = len(payloads)
+    rng = np.random.RandomState(seed + 7919)
+    if rate is None:
+        arrivals = np.zeros(n_requests)
+    else:
+        gaps = rng.exponential(1.0 / rate, size=n_requests)
+        arrivals = np.cumsum(gaps) - gaps[0]
     reqs = []
     for t in range(n_requests):
         reqs.append(dict(tag=t, arrival=float(arrivals[t]), payload=int(rng.randint(pool)),
@@ -314,11 +328,13 @@ def latency_summary(out, voxels=None):
                 mean_s=float(lat.mean()), solves_per_s=len(out) / span, span_s=span)
 
 
-def served_vs_plain(n_requests=96, rate=50.0, pool=8, seed=0, max_resident=None, check=4):
-    """Both loops on one arrival sequence; the first `check` requests' u and
-    iteration counts are compared between them."""
+def served_vs_plain(n_requests=96, rate=50.0, pool=8, seed=0, max_resident=None, check=4, payloads=None):
+    """Both loops on one arrival sequence (rate None: all requests at t = 0,
+    the saturated capacity); the first `check` requests' u and iteration
+    counts are compared between them."""
     import torch
-    payloads, reqs = make_workload(n_requests, rate=rate, pool=pool, seed=seed)
+    payloads, reqs = make_workload(n_requests, rate=rate, pool=pool, seed=seed, payloads=payloads)
+    pool = len(payloads)
     # warm both paths on a small request
     warm = [dict(tag=0, arrival=0.0, payload=int(np.argmin([np.prod(p["shape"]) for p in payloads])),
                  weighting=0.05, decay=30.0)]
@@ -340,10 +356,12 @@ def served_vs_plain(n_requests=96, rate=50.0, pool=8, seed=0, max_resident=None,
         itdiff.append(abs(served[t]["iterations"] - plain[t]["iterations"]))
     vox = [int(np.prod(payloads[r["payload"]]["shape"])) for r in reqs]
     its = [served[r["tag"]]["iterations"] for r in reqs]
-    return dict(workload="%d requests, Poisson arrivals at %g/s, volumes from a pool of %d helix phantoms with "
-                          "sides uniform in 64-320 and noise sigma uniform in 0.1-1.5, (weighting, decay) from the "
-                          "25 x 17 grid, ATV, stop at residual 1e-4 (update 30, at most 3000 iterations)"
-                          % (n_requests, rate, pool),
+    arrivals = "all at t = 0 (saturated)" if rate is None else "Poisson arrivals at %g/s" % rate
+    return dict(workload="%d requests, %s, volumes from a pool of %d helix phantoms with "
+                          "sides uniform in 64-320 per axis and noise sigma uniform in 0.1-1.5 (torch-generated "
+                          "noise), (weighting, decay) from the 25 x 17 grid, ATV, stop at residual 1e-4 "
+                          "(update 30, at most 3000 iterations)" % (n_requests, arrivals, pool),
+                checked_requests=min(check, n_requests),
                 served=latency_summary(served), plain=latency_summary(plain),
                 speedup_solves_per_s=latency_summary(served)["solves_per_s"] / latency_summary(plain)["solves_per_s"],
                 mean_voxels=float(np.mean(vox)), iterations={"median": float(np.median(its)), "max": int(max(its))},
@@ -364,8 +382,10 @@ def _main(argv=None):
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--pool", type=int, default=8)
     ap.add_argument("--max-resident", type=int, default=None)
+    ap.add_argument("--check", type=int, default=4)
     a = ap.parse_args(argv)
-    print(json.dumps(served_vs_plain(a.requests, a.rate, a.pool, max_resident=a.max_resident)))
+    print(json.dumps(served_vs_plain(a.requests, a.rate if a.rate > 0 else None, a.pool, max_resident=a.max_resident,
+                                     check=a.check)))
 
 
 if __name__ == "__main__":

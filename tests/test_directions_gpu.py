@@ -2,10 +2,10 @@
 drop-in AdvancedAdjuster / TransformationCompleter with the oracle.
 
 The kernels follow the reference's rounding sequence (no contracted
-multiply-adds, the quaternion expansion's trigonometry in double), so the
-discrete outputs are compared exactly: ridge maps (at most 1e-4 of the voxels
-may differ through a last-bit difference of the device cos/sin), and the sign
-flips bit-exact given identical ridge inputs.  Completed frames are compared as
+multiply-adds, the quaternion expansion's cos/sin rounded to float from the
+exact values), so the discrete outputs are compared exactly: main directions
+and ridge maps bit for bit (a few tests allow 1e-4 of the voxels), and the
+sign flips bit-exact given identical ridge inputs.  Completed frames are compared as
 rotations (1e-5)."""
 import io
 import contextlib
@@ -94,6 +94,30 @@ def test_kernels_match_oracle_on_random_inputs(shape):
     rd = rng.normal(size=(R, 3)).astype(np.float32)
     for sc in [(1, 1, 1), (0.5, 2.0, 1.25)]:
         assert np.array_equal(_bits(_gpu_adjust(v, coords, rd, sc)), _bits(O.adjust_nonridge_signs(v, coords, rd, sc)))
+
+
+def test_main_directions_and_ridges_bit_exact_on_a_million_quaternions():
+    """The quaternion expansion's cos/sin are the floats nearest to the exact
+    values (single-precision double-float evaluation, double precision where
+    that is not certain): main directions and ridge maps equal the oracle's
+    bit for bit over 1M voxels, including angles beyond [-4, 4] (the double
+    path), half angles at and next to multiples of pi/2, and tiny angles."""
+    from miccai2016_gb300.ridge_detection import RawRidgeDetector
+    rng = np.random.RandomState(11)
+    shape = (64, 128, 128)
+    q = I.random_squeezed(rng, shape).reshape(-1, 3)
+    n = len(q)
+    wide = rng.rand(n) < 0.01
+    q[wide] = rng.uniform(-20, 20, (int(wide.sum()), 3)).astype(np.float32)
+    quarter = np.float32(np.pi / 2) * rng.randint(-2, 3, 4096).astype(np.float32)
+    near = np.nextafter(quarter, np.float32(np.inf) * rng.choice([-1, 1], 4096).astype(np.float32))
+    q[:4096, 1] = 2 * near
+    q[4096:8192, 0] = near
+    q[8192:12288, 2] = rng.uniform(-1e-5, 1e-5, 4096).astype(np.float32)
+    q = q.reshape(shape + (3,))
+    assert np.array_equal(_bits(_gpu_extract(q)), _bits(O.extract_main_directions(q)))
+    resp = rng.uniform(0, 1, shape).astype(np.float32)
+    assert np.array_equal(RawRidgeDetector(None, 0.05).detect(resp, q), O.detect_ridges(resp, q, 0.05))
 
 
 def test_nearest_ridge_ties_go_to_the_lowest_index():

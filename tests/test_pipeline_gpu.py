@@ -5,13 +5,18 @@ pitch 20, noise sigma 1.5 (seed 0); Frangi at sigma 1, 2, 3 with alpha = beta =
 iterations; completion; capacities; an ATV cut of 300 fixed iterations at
 weighting 10^-1.25 and decay 10^1.5.
 
-It runs once through the GPU drop-ins (pipeline.prepare_cut_inputs and
-CmfCutQAnisotropicGpu) and once through the oracle chain (O.frangi,
-misc.normalize, oracle/adjust.advanced_adjuster, O.gvf_run,
-O.complete_transformations, the host capacities, O.maxflow_solve), and the
-results must agree: u within 1e-3 max-abs, the masks at 0.5 on all but 1e-4
-of the voxels, Dice within 1e-3.  The intermediate stages are compared too,
-so that a failure names the stage it starts in."""
+Two comparisons with the oracle chain (O.frangi, misc.normalize,
+oracle/adjust.advanced_adjuster, O.gvf_run, O.complete_transformations, the
+host capacities, O.maxflow_solve):
+  * stage by stage: each GPU stage takes the oracle chain's output of the
+    stage before, so every stage meets its own tolerance on identical inputs
+    and the cut meets the max-flow ones (u within 1e-3 max-abs, masks at 0.5
+    on all but 1e-4 of the voxels, Dice within 1e-3);
+  * end to end: pipeline.prepare_cut_inputs and the cut against the whole
+    oracle chain, where the ridge's discrete decisions let small float
+    differences of the vesselness through (see that test), and the
+    segmentation quality must agree.
+"""
 import contextlib
 import io
 
@@ -61,25 +66,110 @@ def _gpu_chain(noisy, cfg, scales, thresholds):
                 ridge_points=d["ridge_points"])
 
 
-def test_plain_pipeline_64cube_matches_the_oracle_chain():
+def _main_axis(quats):
+    from oracle import oracle as O
+    return O.extract_main_directions(quats)
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
+
+
+def _inputs64():
     from miccai2016_gb300 import phantom as P
     cfg = P.CONFIG_PLAIN_64
-    scales, thresholds = (1, 3, 3), (0.01, 0.3)
     noisy, truth = P.helix_phantom(cfg["shape"], cfg["tube_radius"], cfg["helix_radius"], cfg["pitch"], cfg["sigma"],
                                    cfg["seed"])
-    noisy = noisy.astype(np.float32)
-    o = _oracle_chain(noisy, cfg, scales, thresholds)
-    g = _gpu_chain(noisy, cfg, scales, thresholds)
-    # stage by stage (diagnostic bounds: the tolerances of the per-stage tests)
-    assert np.max(np.abs(g["resp"] - o["resp"])) <= 1e-4, "vesselness"
-    assert g["ridge_points"] == int(o["ridge"].sum()), "cleaned ridge size"
-    # the cut
+    return cfg, noisy.astype(np.float32), truth
+
+
+def test_plain_pipeline_64cube_stage_by_stage_against_the_oracle_chain():
+    """Every GPU stage of the chain takes the oracle chain's output of the
+    stage before it, so the stages are compared on identical inputs at their
+    own tolerances, down to the cut at the max-flow tolerances."""
+    import torch
+    from miccai2016_gb300 import phantom as P
+    from miccai2016_gb300.adjust_directions import AdvancedAdjuster, TransformationCompleter
+    from miccai2016_gb300.capacities import cut_inputs
+    from miccai2016_gb300.continuous_cut_anisotropic_gpu import CmfCutQAnisotropicGpu
+    from miccai2016_gb300.gradient_vector_flow import GvfGpu, GvfParameters
+    from miccai2016_gb300.misc import normalize
+    from miccai2016_gb300.qfrangi_gpu import FeatureFilter, VesselnessCalculation
+    from oracle import adjust as A
+    from oracle import oracle as O
+    cfg, noisy, truth = _inputs64()
+    # Frangi
+    val_o, quat_o, _ = O.frangi(noisy, (1, 3, 3))
+    resp_o = normalize(val_o, dst_min=0.0, dst_max=1.0, perc_low=None, perc_up=None, clip=True)
+    vp = VesselnessCalculation.Parameters()
+    vp.bright_objects, vp.scales = True, (1, 3, 3)
+    val_g, quat_g, _ = FeatureFilter(vp).execute_for(noisy, roi=None, voxel_size=(1, 1, 1))
+    resp_g = normalize(val_g, dst_min=0.0, dst_max=1.0, perc_low=None, perc_up=None, clip=True)
+    assert np.max(np.abs(resp_g - resp_o)) <= 1e-4
+    cos_q = np.abs(np.sum(_main_axis(quat_g) * _main_axis(quat_o), axis=-1))
+    assert np.mean(cos_q < 1 - 1e-3) <= 1e-3
+    # sign adjustment on the oracle's Frangi output: every sign, every bit
+    with contextlib.redirect_stdout(io.StringIO()):
+        adj_o, ridge_o, _ = A.advanced_adjuster(quat_o, resp_o, (0.01, 0.3))
+        adjuster = AdvancedAdjuster((0.01, 0.3), quat_o, resp_o, voxel_size=(1, 1, 1))
+        adj_g = adjuster.execute(verbose=False)
+    assert np.array_equal(adjuster.ridge, ridge_o)
+    assert np.array_equal(_bits(adj_g), _bits(adj_o))
+    # GVF on the oracle's adjusted directions
+    scaled = np.rollaxis(np.rollaxis(adj_o, -1) * resp_o, 0, adj_o.ndim)
+    g_o, _, _ = O.gvf_run(scaled, cfg["gvf_mu"], cfg["gvf_iter"], cfg["gvf_iter"] // 10, tol=0.0, normalize=False)
+    gp = GvfParameters()
+    gp.mu, gp.tol, gp.maxiter, gp.callback, gp.update, gp.normalize = (cfg["gvf_mu"], 0, cfg["gvf_iter"], None,
+                                                                       cfg["gvf_iter"] // 10, False)
+    g_g = GvfGpu(scaled, gp, (1, 1, 1)).execute()
+    mag = float(np.max(np.linalg.norm(g_o, axis=-1)))
+    assert np.max(np.abs(g_g - g_o)) <= 1e-4 * mag
+    # completion on the oracle's GVF field
+    q_o = O.complete_transformations(g_o)
+    q_g = TransformationCompleter(g_o).complete()
+    cos_c = np.abs(np.sum(_main_axis(q_g) * _main_axis(q_o), axis=-1))
+    assert np.min(cos_c) >= 1 - 1e-5
+    # capacities
+    bgw_o, fgw_o = P.bgfg_weights(noisy, cfg["sigma"])
+    fgw_g, bgw_g, grad2_g = cut_inputs(noisy, cfg["sigma"])
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    assert np.max(np.abs(fgw_g - f(fgw_o))) <= 4 * np.finfo(np.float32).eps * max(1.0, float(np.max(fgw_o)))
+    assert np.max(np.abs(bgw_g - f(bgw_o))) <= 4 * np.finfo(np.float32).eps * max(1.0, float(np.max(bgw_o)))
+    assert np.array_equal(grad2_g, f(P.grad_mag_sq(noisy)))
+    # the cut on the oracle's quaternions and capacities
+    alpha = f(P.nonterminal_weights(P.grad_mag_sq(noisy), cfg["weighting"], cfg["decay"]))
+    u_o, it_o, _ = O.maxflow_solve(noisy, q_o, P.ATV_EIGS, alpha, f(fgw_o), f(bgw_o), num_iter=cfg["num_iter"],
+                                   update=30, error_bound=-1.0)
+    p = CmfCutQAnisotropicGpu.CutParameters()
+    p.num_iter, p.update, p.error_bound = cfg["num_iter"], 30, -1.0
+    cutter = CmfCutQAnisotropicGpu(p)
+    u_g = cutter.execute(noisy, q_o, P.ATV_EIGS, alpha, f(fgw_o), f(bgw_o), verbose=False)
+    assert cutter.last_iterations == it_o == cfg["num_iter"]
+    assert np.max(np.abs(u_g - u_o)) <= U_TOL
+    assert np.mean((u_g >= 0.5) != (u_o >= 0.5)) <= MASK_FRAC
+    assert abs(P.fast_dice(u_g, truth) - P.fast_dice(u_o, truth)) <= DICE_TOL
+    torch.cuda.synchronize()
+
+
+def test_plain_pipeline_64cube_end_to_end_against_the_oracle_chain():
+    """The whole chain on each side (pipeline.prepare_cut_inputs and the
+    cut against the oracle chain).  Vesselness agrees within 1e-6, but the
+    ridge is a set of discrete decisions (a response against its
+    interpolated neighbours) and a few of them fall the other way: 27,008
+    against 26,999 points after cleaning.  The sign propagation and the GVF
+    spread such differences over whole segments, so u is not comparable
+    voxel by voxel; what must agree is the segmentation quality."""
+    from miccai2016_gb300 import phantom as P
+    cfg, noisy, truth = _inputs64()
+    o = _oracle_chain(noisy, cfg, (1, 3, 3), (0.01, 0.3))
+    g = _gpu_chain(noisy, cfg, (1, 3, 3), (0.01, 0.3))
+    ridge_o = int(o["ridge"].sum())
+    d = dict(resp=float(np.max(np.abs(g["resp"] - o["resp"]))), ridge=(g["ridge_points"], ridge_o),
+             dice=(P.fast_dice(g["u"], truth), P.fast_dice(o["u"], truth)),
+             dice_largest=(P.dice_largest(g["u"], truth), P.dice_largest(o["u"], truth)))
+    print("pipeline 64^3 end to end:", d)
+    assert d["resp"] <= 1e-4, d
+    assert abs(g["ridge_points"] - ridge_o) <= 1e-3 * ridge_o, d
     assert g["iterations"] == o["iterations"] == cfg["num_iter"]
-    du = float(np.max(np.abs(g["u"] - o["u"])))
-    mask_g, mask_o = g["u"] >= 0.5, o["u"] >= 0.5
-    mask_frac = float(np.mean(mask_g != mask_o))
-    dice_g, dice_o = P.fast_dice(g["u"], truth), P.fast_dice(o["u"], truth)
-    assert du <= U_TOL, ("u", du)
-    assert mask_frac <= MASK_FRAC, ("mask", mask_frac)
-    assert abs(dice_g - dice_o) <= DICE_TOL, ("dice", dice_g, dice_o)
-    assert dice_o > 0.4   # the pipeline segments the tube at all (0.50 after 300 iterations)
+    assert abs(d["dice"][0] - d["dice"][1]) <= 0.02, d
+    assert min(d["dice"]) > 0.4, d
