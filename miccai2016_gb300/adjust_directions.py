@@ -22,7 +22,7 @@ import time
 import numpy as np
 
 from . import _native as N
-from .labeling import label26
+from .labeling import label26, label_device
 from .parameters import TreePrintable
 from .ridge_detection import RawRidgeDetector, hysteresis_threshold
 from .ridge_mst import propagate_signs, ridge_mst_edges
@@ -130,6 +130,9 @@ class AdvancedAdjuster(TreePrintable):
     @property
     def main_dirs_unadjusted(self):
         """After execute(): the extracted, not yet adjusted main directions."""
+        if self.__main_dirs_unadjusted is None and getattr(self, "_d_main_unadjusted", None) is not None:
+            self.__main_dirs_unadjusted = self._d_main_unadjusted.cpu().numpy()
+            self._d_main_unadjusted = None
         return self.__main_dirs_unadjusted
 
     # -- the sequence (adjust_directions.py:213-256) ---------------------------
@@ -140,6 +143,18 @@ class AdvancedAdjuster(TreePrintable):
         torch = N.torch_mod()
         self.timings = {}   # seconds per step of the last execute()
         self._d_qeigs = N.to_device_f32(self.qeigs)
+        if self.labeler == "gpu" and self.mst_local == "gpu":
+            adjusted = self._execute_device()
+        else:
+            adjusted = self._execute_host()
+        del self._d_qeigs
+        self._d_main = None
+        torch.cuda.current_stream().synchronize()
+        return adjusted
+
+    def _execute_host(self):
+        """The sequence with the volumes on the host (labeler or mst_local
+        "host"): each step as the reference writes it."""
         with self._timed("ridge_candidates_and_hysteresis"):
             labeled_ridge = self._label_ridge()
         adjusted = None
@@ -156,10 +171,121 @@ class AdvancedAdjuster(TreePrintable):
             if not self.ridge_detection_only:
                 with self._timed("nearest_ridge_flip"):
                     adjusted = self._adjust_all_directions(ridge_coords, ridge_dirs)
-        del self._d_qeigs
-        self._d_main = None
-        torch.cuda.current_stream().synchronize()
+                self.ridge_coords, self.ridge_dirs = ridge_coords, ridge_dirs
         return adjusted
+
+    def _execute_device(self):
+        """The same sequence with every volume kept on the device: ridge
+        candidates, hysteresis, the main directions, the labels of the
+        cleaning and the cleaned ridge stay there, and only lists of ridge
+        points (coordinates, their directions and labels) come to the host
+        for the tree steps.  Gives _execute_host's bits."""
+        self.__main_dirs_unadjusted = None
+        self._d_main_unadjusted = None
+        with self._timed("ridge_candidates_and_hysteresis"):
+            d_ridge = self._label_ridge_dev()
+        adjusted = None
+        if (not self.ridge_detection_only) or self.clean_ridge:
+            with self._timed("main_directions"):
+                d_main = self._d_main
+                self._d_main_unadjusted = d_main
+                self._d_qeigs.copy_(d_main)
+                self._d_main = None
+            pts = self._ridge_points_dev(d_ridge)
+            ridge_coords, ridge_dirs = self._adjust_ridge_directions_dev(pts, d_main,
+                                                                         join_components=not self.clean_ridge)
+            if self.clean_ridge:
+                d_ridge = self._do_clean_ridge_dev(d_ridge, pts, ridge_dirs)
+                if not self.ridge_detection_only:
+                    pts = self._ridge_points_dev(d_ridge)
+                    ridge_coords, ridge_dirs = self._adjust_ridge_directions_dev(pts, d_main)
+            if not self.ridge_detection_only:
+                with self._timed("nearest_ridge_flip"):
+                    adjusted = self._adjust_all_directions(ridge_coords, ridge_dirs)
+                self.ridge_coords, self.ridge_dirs = ridge_coords, ridge_dirs
+        with self._timed("ridge_to_host"):
+            self.__ridge = d_ridge.to(N.torch_mod().float32).cpu().numpy()
+        return adjusted
+
+    def _label_ridge_dev(self):
+        """Ridge candidates and main directions in one pass
+        (m16_detect_ridges_main_directions), then the hysteresis (m16_hysteresis)
+        on the device.  Returns the ridge as a uint8 device mask; the main
+        directions stay in self._d_main."""
+        torch = N.torch_mod()
+        L = N.lib()
+        shape = tuple(int(v) for v in self.response.shape)
+        resp = N.to_device_f32(self.response, shape)
+        d_ridge = torch.empty(shape, dtype=torch.float32, device=N.device())
+        self._d_main = torch.empty_like(self._d_qeigs)
+        st = L.m16_detect_ridges_main_directions(N.ptr(resp), N.ptr(self._d_qeigs), shape[0], shape[1], shape[2],
+                                                 float(self._ridge_detector.threshold), N.ptr(d_ridge),
+                                                 N.ptr(self._d_main), N.stream_ptr())
+        N.check("m16_detect_ridges_main_directions", st)
+        cand = (d_ridge != 0).to(torch.uint8)
+        if not self._hysteresis:
+            return cand
+        # sure = ridge & (response >= upper), compared in float32 as numpy does
+        sure = (cand.bool() & (resp >= self.threshold[1])).to(torch.uint8)
+        out = torch.empty(shape, dtype=torch.uint8, device=N.device())
+        ws = N.workspace(L.m16_hysteresis_workspace_bytes(*shape))
+        N.check("m16_hysteresis", L.m16_hysteresis(N.ptr(cand), N.ptr(sure), shape[0], shape[1], shape[2], N.ptr(out),
+                                                   N.ptr(ws), ws.numel(), N.stream_ptr()))
+        return out
+
+    def _ridge_points_dev(self, d_mask):
+        """(host int64 R x 3, device int64 R x 3) coordinates of the mask's
+        voxels in C order (np.argwhere's order)."""
+        with self._timed("ridge_coordinates"):
+            d_coords = N.torch_mod().nonzero(d_mask)
+            return d_coords.cpu().numpy(), d_coords
+
+    def _adjust_ridge_directions_dev(self, pts, d_main, join_components=True):
+        """_adjust_ridge_directions on the device mask: the directions are
+        gathered at the ridge points on the device."""
+        coords, d_coords = pts
+        if len(coords) == 0:
+            raise ValueError("no ridge points: nothing to propagate directions along")
+        with self._timed("mst_local" if not join_components else "mst_local_and_joins"):
+            a, b = ridge_mst_edges(coords, self.voxel_size, join_components=join_components, local=self.mst_local)
+        with self._timed("sign_propagation"):
+            dirs = d_main[d_coords[:, 0], d_coords[:, 1], d_coords[:, 2]].cpu().numpy()
+            adjusted = propagate_signs(len(coords), a, b, dirs)
+        return np.asarray(coords, dtype=np.uint16, order="C"), adjusted
+
+    def _do_clean_ridge_dev(self, d_mask, pts, ridge_dirs):
+        """_do_clean_ridge on the device mask: labels on the device, the
+        per-segment sums from the labels at the ridge points, the kept
+        segments selected on the device.  Returns the cleaned uint8 mask."""
+        torch = N.torch_mod()
+        coords, d_coords = pts
+        scaled = ridge_dirs * self.__voxel_size   # float32 * tuple -> float64, as in the reference
+        with self._timed("clean_labels"):
+            d_comp, n_lab = label_device(d_mask, 26)
+            point_label = d_comp[d_coords[:, 0], d_coords[:, 1], d_coords[:, 2]].cpu().numpy()
+        with self._timed("clean_segment_sums"):
+            kept = self._kept_segments(point_label, n_lab, len(coords) < d_mask.numel(), scaled)
+        keep = np.zeros(n_lab + 1, dtype=np.uint8)
+        keep[np.asarray(kept, dtype=np.int64)] = 1
+        return torch.from_numpy(keep).to(N.device())[d_comp.long()]
+
+    def _kept_segments(self, point_label, n_lab, has_background, scaled):
+        """The labels the cleaning keeps (adjust_directions.py:319-337): the
+        ceil(3 ln(e + n)) segments with the longest summed (scaled) direction,
+        the sort stable on ties.  Per segment the directions are summed in
+        the C order of its voxels, one after the other (np.sum over axis 0
+        of the reference's list, and np.bincount, add sequentially)."""
+        # np.unique(components)[1:] without the sort: the labels are 1..n_lab,
+        # and "[1:]" drops label 1 too when no voxel is background
+        labels = np.arange(1 if has_background else 2, n_lab + 1)
+        sums = np.stack([np.bincount(point_label, weights=scaled[:, k], minlength=n_lab + 1) for k in range(3)], -1)
+        lengths = {}
+        for lab in labels:
+            lengths[lab] = np.linalg.norm(sums[lab])
+        ordered = sorted(lengths, key=lambda k: lengths[k], reverse=True)
+        boundary = int(np.ceil(3 * np.log(np.e + len(ordered))))
+        print("Keeping %s of %s labels." % (boundary, len(ordered)))
+        return ordered[:boundary]
 
     class _Timer(object):
         def __init__(self, timings, name):
@@ -204,24 +330,9 @@ class AdvancedAdjuster(TreePrintable):
         scaled = ridge_dirs * self.__voxel_size   # float32 * tuple -> float64, as in the reference
         with self._timed("clean_labels"):
             components, n_lab = label26(labeled_ridge, where=self.labeler)
-        t_sums = self._timed("clean_segment_sums")
-        t_sums.__enter__()
-        # np.unique(components)[1:] without the sort: the labels are 1..n_lab,
-        # and "[1:]" drops label 1 too when no voxel is background
-        labels = np.arange(1 if len(ridge_coords) < components.size else 2, n_lab + 1)
-        point_label = components[tuple(np.asarray(ridge_coords, np.intp).T)]
-        order = np.argsort(point_label, kind="stable")
-        sorted_labels = point_label[order]
-        starts = np.searchsorted(sorted_labels, labels, side="left")
-        ends = np.searchsorted(sorted_labels, labels, side="right")
-        lengths = {}
-        for lab, s, e in zip(labels, starts, ends):
-            lengths[lab] = np.linalg.norm(np.sum(scaled[order[s:e]], axis=0))
-        ordered = sorted(lengths, key=lambda k: lengths[k], reverse=True)
-        boundary = int(np.ceil(3 * np.log(np.e + len(ordered))))
-        t_sums.__exit__()
-        print("Keeping %s of %s labels." % (boundary, len(ordered)))
-        kept = ordered[:boundary]
+        with self._timed("clean_segment_sums"):
+            point_label = components[tuple(np.asarray(ridge_coords, np.intp).T)]
+            kept = self._kept_segments(point_label, n_lab, len(ridge_coords) < components.size, scaled)
         keep = np.zeros(n_lab + 1, dtype=bool)   # np.in1d(components, kept) as a table lookup
         keep[np.asarray(kept, dtype=np.int64)] = True
         cleaned = keep[components].astype(labeled_ridge.dtype).reshape(components.shape)

@@ -46,6 +46,27 @@ def label(mask, connectivity=26, where="gpu"):
     return out.cpu().numpy(), int(n.value)
 
 
+def label_device(mask, connectivity=26):
+    """(labels int32 CUDA tensor, number of components) of a 3-D uint8 (or
+    bool) CUDA tensor mask: label() without leaving the device."""
+    torch = N.torch_mod()
+    L = N.lib()
+    if mask.dim() != 3:
+        raise ValueError("mask must be three-dimensional")
+    if connectivity not in (6, 26):
+        raise ValueError("connectivity must be 6 or 26")
+    m = mask if mask.dtype == torch.uint8 else (mask != 0).to(torch.uint8)
+    m = m.contiguous()
+    d0, d1, d2 = (int(s) for s in m.shape)
+    out = torch.empty((d0, d1, d2), dtype=torch.int32, device=m.device)
+    ws = N.workspace(L.m16_label_workspace_bytes(d0, d1, d2))
+    n = ctypes.c_int32(0)
+    st = L.m16_label(N.ptr(m), d0, d1, d2, int(connectivity), N.ptr(out), ctypes.byref(n), N.ptr(ws), ws.numel(),
+                     N.stream_ptr())
+    N.check("m16_label", st)
+    return out, int(n.value)
+
+
 def label26(mask, where="gpu"):
     """label(mask, 26, where): the labelling of the sign adjustment."""
     return label(mask, 26, where)

@@ -172,11 +172,9 @@ class _AdjusterFromOracleRidge(object):
         from miccai2016_gb300.adjust_directions import AdvancedAdjuster
 
         class Adj(AdvancedAdjuster):
-            def _label_ridge(self):
+            def _label_ridge_dev(self):
                 self._d_main = torch.from_numpy(np.ascontiguousarray(main)).to(N.device())
-                ridge = np.require(ridge_h, np.float32, ["C", "A", "W"]).copy()
-                self._AdvancedAdjuster__ridge = ridge
-                return ridge
+                return torch.from_numpy(np.ascontiguousarray(ridge_h != 0, dtype=np.uint8)).to(N.device())
 
         return Adj(th, quat, resp, voxel_size=(1, 1, 1))
 
@@ -192,6 +190,24 @@ def test_advanced_adjuster_signs_bit_exact_from_the_oracle_ridge(th):
     assert ridge_o.sum() > 0
     assert np.array_equal(obj.ridge, ridge_o)                  # the cleaning keeps the same segments
     assert np.array_equal(_bits(adj), _bits(adj_o))            # every sign, every bit
+
+
+def test_device_and_host_sequences_give_the_same_bits():
+    """execute() keeps the volumes on the device by default; the host
+    sequence (labelling and the MST's local phase on the host) gives the
+    same ridge and the same adjusted directions, bit for bit."""
+    from miccai2016_gb300.adjust_directions import AdvancedAdjuster
+    resp, quat = _small_tube()
+    for th, clean in (((0.05, 0.3), True), ((0.2, 0.5), False), (0.1, True)):
+        with contextlib.redirect_stdout(io.StringIO()):
+            dev = AdvancedAdjuster(th, quat, resp, voxel_size=(1, 1, 1), clean_ridge=clean)
+            a_dev = dev.execute(verbose=False)
+            host = AdvancedAdjuster(th, quat, resp, voxel_size=(1, 1, 1), clean_ridge=clean)
+            host.labeler, host.mst_local = "host", "host"
+            a_host = host.execute(verbose=False)
+        assert np.array_equal(dev.ridge, host.ridge)
+        assert np.array_equal(_bits(a_dev), _bits(a_host))
+        assert np.array_equal(_bits(dev.main_dirs_unadjusted), _bits(host.main_dirs_unadjusted))
 
 
 def test_ridge_detection_only_and_no_cleaning():
