@@ -499,6 +499,36 @@ int m16_compose_signs(int64_t n, const int32_t *order, int64_t n_order, const in
 int m16_tree_order(int64_t n, const int32_t *ea, const int32_t *eb, int64_t n_edges, int32_t root, int32_t *order,
                    int32_t *pred);
 
+/*
+ * The same propagation on the device, in two calls.  Replaces the visit of
+ * AdvancedAdjuster._adjust_ridge_directions (src/processing/adjust_directions.py:382-415)
+ * from root point 0; every other tree of a forest starts at its lowest-index
+ * point.
+ *
+ * m16_ridge_edge_codes: per edge (edges_a[k] -- edges_b[k], device int32,
+ * num_edges < num_points) the sign code of the float32 dot product of the two
+ * points' directions (dirs3: device float32, num_points x 3): 1, -1, 0, 2
+ * (NaN), 3 where the float32 rounding of the dot could decide the sign (the
+ * caller evaluates those with the reference's own np.dot and writes 1, -1 or
+ * 0), 4 for an endpoint outside [0, num_points).  codes: device int8.
+ */
+int m16_ridge_edge_codes(const float *dirs3, int64_t num_points, const int32_t *edges_a, const int32_t *edges_b,
+                         int64_t num_edges, int8_t *codes, void *stream);
+
+/* Workspace bytes of m16_ridge_signs (0 for invalid sizes). */
+size_t m16_ridge_signs_workspace_bytes(int64_t num_points, int64_t num_edges);
+
+/*
+ * m16_ridge_signs: the final sign (device int8, num_points) of every point's
+ * direction, from the edges of a forest and their codes (each 1, -1, 0 or 2;
+ * anything else returns M16_ERR_BAD_ARG): a parity union-find over the 1 / -1
+ * edges on the device, the pieces between zero and NaN edges ordered on the
+ * host.  Equal to m16_tree_order + m16_compose_signs from root 0.
+ * Synchronizes `stream`.
+ */
+int m16_ridge_signs(int64_t num_points, const int32_t *edges_a, const int32_t *edges_b, const int8_t *codes,
+                    int64_t num_edges, int8_t *signs, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- 26-connected labelling ------------------------------------------------------ */
 
 /* Workspace bytes of m16_label26 (0 for invalid sizes). */

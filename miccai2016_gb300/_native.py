@@ -128,6 +128,12 @@ def _declare(L):
     L.m16_tree_order.argtypes = [_i64, _vp, _vp, _i64, _i32, _vp, _vp]
     L.m16_compose_signs.restype = ctypes.c_int
     L.m16_compose_signs.argtypes = [_i64, _vp, _i64, _vp, _vp, _vp]
+    L.m16_ridge_edge_codes.restype = ctypes.c_int
+    L.m16_ridge_edge_codes.argtypes = [_vp, _i64, _vp, _vp, _i64, _vp, _vp]
+    L.m16_ridge_signs_workspace_bytes.restype = ctypes.c_size_t
+    L.m16_ridge_signs_workspace_bytes.argtypes = [_i64, _i64]
+    L.m16_ridge_signs.restype = ctypes.c_int
+    L.m16_ridge_signs.argtypes = [_i64, _vp, _vp, _vp, _i64, _vp, _vp, ctypes.c_size_t, _vp]
     L.m16_label26_workspace_bytes.restype = _sz
     L.m16_label26_workspace_bytes.argtypes = [_i32, _i32, _i32]
     L.m16_label26.restype = ctypes.c_int

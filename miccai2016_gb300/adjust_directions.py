@@ -25,7 +25,7 @@ from . import _native as N
 from .labeling import label26, label_device
 from .parameters import TreePrintable
 from .ridge_detection import RawRidgeDetector, hysteresis_threshold
-from .ridge_mst import propagate_signs, ridge_mst_edges
+from .ridge_mst import propagate_signs, propagate_signs_device, ridge_mst_edges
 
 
 class AdvancedAdjuster(TreePrintable):
@@ -249,8 +249,8 @@ class AdvancedAdjuster(TreePrintable):
         with self._timed("mst_local" if not join_components else "mst_local_and_joins"):
             a, b = ridge_mst_edges(coords, self.voxel_size, join_components=join_components, local=self.mst_local)
         with self._timed("sign_propagation"):
-            dirs = d_main[d_coords[:, 0], d_coords[:, 1], d_coords[:, 2]].cpu().numpy()
-            adjusted = propagate_signs(len(coords), a, b, dirs)
+            d_dirs = d_main[d_coords[:, 0], d_coords[:, 1], d_coords[:, 2]]
+            adjusted = propagate_signs_device(d_dirs, a, b).cpu().numpy()
         return np.asarray(coords, dtype=np.uint16, order="C"), adjusted
 
     def _do_clean_ridge_dev(self, d_mask, pts, ridge_dirs):

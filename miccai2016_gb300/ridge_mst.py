@@ -262,3 +262,39 @@ def propagate_signs(n, edges_a, edges_b, dirs, root=0):
     neg = val[:, None] < 0
     adjusted[:] = np.where(neg, -dirs, dirs)   # negation flips the sign bit, NaN too
     return adjusted
+
+
+def propagate_signs_device(d_dirs, edges_a, edges_b):
+    """propagate_signs from root 0 on the device: d_dirs (CUDA float32
+    tensor, n x 3), the forest's edges (host or device int arrays).  Every
+    edge's dot-product sign comes from m16_ridge_edge_codes; the few whose
+    float32 rounding could decide the sign are evaluated with np.dot itself,
+    as the reference's loop evaluates them; m16_ridge_signs composes the signs
+    (a parity union-find over the +-1 edges).  Returns the adjusted
+    directions as a CUDA tensor, bit for bit propagate_signs(n, a, b, dirs)."""
+    torch = N.torch_mod()
+    L = N.lib()
+    n = int(d_dirs.shape[0])
+    dev = d_dirs.device
+    d_dirs = d_dirs.contiguous()
+    to_dev = lambda e: (e.to(device=dev, dtype=torch.int32) if N.is_torch(e)
+                        else torch.from_numpy(np.ascontiguousarray(e, dtype=np.int32)).to(dev))
+    d_a, d_b = to_dev(edges_a), to_dev(edges_b)
+    ne = int(d_a.numel())
+    codes = torch.empty(max(ne, 1), dtype=torch.int8, device=dev)
+    N.check("m16_ridge_edge_codes", L.m16_ridge_edge_codes(N.ptr(d_dirs), n, N.ptr(d_a), N.ptr(d_b), ne,
+                                                           N.ptr(codes), N.stream_ptr()))
+    unsure = torch.nonzero(codes[:ne] == 3).flatten()
+    if unsure.numel():
+        ca = d_dirs[d_a[unsure].long()].cpu().numpy()
+        cb = d_dirs[d_b[unsure].long()].cpu().numpy()
+        fixed = np.empty(len(ca), np.int8)
+        for k in range(len(ca)):
+            d = np.dot(ca[k], cb[k])   # the float32 np.dot of the reference's loop (commutative)
+            fixed[k] = 1 if d > 0 else (-1 if d < 0 else 0)
+        codes[unsure] = torch.from_numpy(fixed).to(dev)
+    signs = torch.empty(n, dtype=torch.int8, device=dev)
+    ws = N.workspace(L.m16_ridge_signs_workspace_bytes(n, ne))
+    N.check("m16_ridge_signs", L.m16_ridge_signs(n, N.ptr(d_a), N.ptr(d_b), N.ptr(codes), ne, N.ptr(signs), N.ptr(ws),
+                                                 ws.numel(), N.stream_ptr()))
+    return torch.where(signs[:, None] < 0, -d_dirs, d_dirs)
