@@ -297,4 +297,8 @@ def propagate_signs_device(d_dirs, edges_a, edges_b):
     ws = N.workspace(L.m16_ridge_signs_workspace_bytes(n, ne))
     N.check("m16_ridge_signs", L.m16_ridge_signs(n, N.ptr(d_a), N.ptr(d_b), N.ptr(codes), ne, N.ptr(signs), N.ptr(ws),
                                                  ws.numel(), N.stream_ptr()))
-    return torch.where(signs[:, None] < 0, -d_dirs, d_dirs)
+    # negate by flipping the sign bit, as numpy's unary minus does (NaN
+    # included: arithmetic on the GPU would return the canonical NaN)
+    flip = torch.where(signs[:, None] < 0, torch.tensor(-2 ** 31, dtype=torch.int32, device=dev),
+                       torch.tensor(0, dtype=torch.int32, device=dev))
+    return torch.bitwise_xor(d_dirs.view(torch.int32), flip).view(torch.float32)
