@@ -529,6 +529,28 @@ size_t m16_ridge_signs_workspace_bytes(int64_t num_points, int64_t num_edges);
 int m16_ridge_signs(int64_t num_points, const int32_t *edges_a, const int32_t *edges_b, const int8_t *codes,
                     int64_t num_edges, int8_t *signs, void *workspace, size_t workspace_bytes, void *stream);
 
+/* Workspace bytes of m16_ridge_forest_joins (0 for invalid sizes). */
+size_t m16_ridge_forest_joins_workspace_bytes(int64_t num_points);
+
+/*
+ * The global phase of the ridge-point tree on the device for unit voxel size:
+ * the edges that join the trees of a forest (its local phase, from
+ * m16_ridge_mst_local) the way Kruskal over all pairs in (weight, i, j)
+ * order joins them -- the tree of minimum_spanning_tree(squareform(pdist(...)))
+ * in AdvancedAdjuster._adjust_ridge_directions (src/processing/adjust_directions.py:374-379).
+ * pts3: device int32 num_points x 3, coordinates in [0, 32767]; edges_a,
+ * edges_b: device int32, the forest.  The least point pair of every two trees
+ * is found exactly (integer squared distances, ties to the lowest indices);
+ * the search compares every tree's points with those of the trees ranked
+ * below it by size, and returns M16_ERR_TOO_LARGE, writing nothing, when that
+ * takes more than max_pair_evaluations distance evaluations.  join_a, join_b
+ * (host int32, capacity num_points - 1), *num_joins (host): the joining
+ * edges, the lower index first.  Synchronizes `stream`.
+ */
+int m16_ridge_forest_joins(const int32_t *pts3, int64_t num_points, const int32_t *edges_a, const int32_t *edges_b,
+                           int64_t num_edges, int64_t max_pair_evaluations, int32_t *join_a, int32_t *join_b,
+                           int64_t *num_joins, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- 26-connected labelling ------------------------------------------------------ */
 
 /* Workspace bytes of m16_label26 (0 for invalid sizes). */

@@ -22,6 +22,7 @@ M16_ERR_BAD_ARG = 2
 M16_ERR_WORKSPACE = 3
 M16_ERR_CUDA = 4
 M16_ERR_TIMEOUT = 5
+M16_ERR_TOO_LARGE = 6
 
 _lock = threading.Lock()
 _lib = None
@@ -132,6 +133,10 @@ def _declare(L):
     L.m16_ridge_edge_codes.argtypes = [_vp, _i64, _vp, _vp, _i64, _vp, _vp]
     L.m16_ridge_signs_workspace_bytes.restype = ctypes.c_size_t
     L.m16_ridge_signs_workspace_bytes.argtypes = [_i64, _i64]
+    L.m16_ridge_forest_joins_workspace_bytes.restype = ctypes.c_size_t
+    L.m16_ridge_forest_joins_workspace_bytes.argtypes = [_i64]
+    L.m16_ridge_forest_joins.restype = ctypes.c_int
+    L.m16_ridge_forest_joins.argtypes = [_vp, _i64, _vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp]
     L.m16_ridge_signs.restype = ctypes.c_int
     L.m16_ridge_signs.argtypes = [_i64, _vp, _vp, _vp, _i64, _vp, _vp, ctypes.c_size_t, _vp]
     L.m16_label26_workspace_bytes.restype = _sz

@@ -1,4 +1,7 @@
-// ridge_signs.cu -- the sign propagation of the ridge directions on the GPU.
+// ridge_forest.cu -- the forest steps of the sign adjustment on the GPU: the
+// sign propagation of the ridge directions along the minimum spanning tree,
+// and the joins of the local trees of that tree (m16_ridge_forest_joins,
+// below the propagation).
 //
 // AdvancedAdjuster._adjust_ridge_directions (src/processing/adjust_directions.py:382-415)
 // walks the minimum spanning tree of the ridge points from point 0 and keeps
@@ -110,7 +113,7 @@ __global__ void rs_union_kernel(const int32_t *__restrict__ ea, const int32_t *_
                                 unsigned long long *err, unsigned long long *bad)
 {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        const int8_t c = codes[k];
+        const int8_t c = codes ? codes[k] : (int8_t)1;   // no codes: every edge joins with parity 0
         if (c != 1 && c != -1) continue;
         if (ea[k] < 0 || ea[k] >= R || eb[k] < 0 || eb[k] >= R) {
             atomicAdd(bad, 1ull);
@@ -369,5 +372,342 @@ extern "C" int m16_ridge_signs(int64_t num_points, const int32_t *edges_a, const
     rs_tops_kernel<<<gr, kRsBlock, 0, st>>>(root, R, pmin, top, tsign);
     rs_signs_kernel<<<gr, kRsBlock, 0, st>>>(root, par, R, top, tsign, signs);
     M16_CUDA_TRY(cudaGetLastError());
+    return M16_OK;
+}
+
+// ---- joins of the local trees -----------------------------------------------------
+//
+// The ridge-point tree is SciPy's Kruskal over all pairs in (weight, i, j)
+// order (adjust_directions.py:374-379).  Its local phase (m16_ridge_mst_local)
+// reproduces it up to weight r; what remains is to join the local trees as
+// the full Kruskal would: Kruskal over the components, each pair of
+// components weighted by its least point pair in (weight, i, j) order.  With
+// unit voxel size every squared distance is an integer and the weights
+// sqrt(d^2) order like d^2 (distinct integers below 2^32 have distinct
+// double square roots), so the least pair of two components is the least
+// (d^2, lo, hi), found exactly in integer arithmetic: the components are
+// ranked by size, and the points of each rank are compared with every point
+// of the lower-ranked (smaller) components, keeping per query point its
+// nearest target point with the lowest index.  A ridge of one large segment
+// and a few small ones costs |large| x |small| integer distance evaluations.
+
+namespace m16 {
+namespace {
+
+constexpr int kFjChunk = 2048;          // target points per block, staged in shared memory
+constexpr int kFjScanItems = 1024;      // points per block of the component numbering
+constexpr int64_t kFjMaxCoord = 32767;  // |dz|^2 + |dy|^2 + |dx|^2 < 2^32
+
+// roots per block of kFjScanItems points (a root is its component's lowest
+// point); 4 consecutive points per thread, as fj_root_id_kernel takes them
+__global__ void __launch_bounds__(256) fj_root_count_kernel(const uint32_t *__restrict__ root, int64_t R,
+                                                            unsigned *__restrict__ bcount)
+{
+    __shared__ unsigned tot;
+    if (threadIdx.x == 0) tot = 0;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * kFjScanItems + 4 * threadIdx.x;
+    unsigned c = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int64_t v = base + j;
+        c += (v < R && root[v] == (uint32_t)v) ? 1u : 0u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&tot, c);
+    __syncthreads();
+    if (threadIdx.x == 0) bcount[blockIdx.x] = tot;
+}
+
+// number of each root in index order: boff[block] + roots before it in the block
+__global__ void __launch_bounds__(256) fj_root_id_kernel(const uint32_t *__restrict__ root, int64_t R,
+                                                         const unsigned *__restrict__ boff, int32_t *__restrict__ cid)
+{
+    __shared__ unsigned warp_tot[8];
+    const int64_t base = (int64_t)blockIdx.x * kFjScanItems + 4 * threadIdx.x;   // 4 consecutive points per thread
+    unsigned flags = 0, cnt = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int64_t v = base + j;
+        const unsigned f = (v < R && root[v] == (uint32_t)v) ? 1u : 0u;
+        flags |= f << j;
+        cnt += f;
+    }
+    // exclusive scan of cnt over the block's 256 threads
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    unsigned before = 0;
+    for (int k = 0; k < w; ++k) before += warp_tot[k];
+    unsigned id = boff[blockIdx.x] + before + x - cnt;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (flags & (1u << j)) cid[base + j] = (int32_t)id++;
+}
+
+// component of every point, the component sizes, coordinates in range
+__global__ void fj_comp_kernel(const uint32_t *__restrict__ root, const int32_t *__restrict__ cid,
+                               const int32_t *__restrict__ pts, int64_t R, int32_t *__restrict__ comp,
+                               unsigned *__restrict__ size, unsigned long long *bad)
+{
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < R; v += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t c = cid[root[v]];
+        comp[v] = c;
+        atomicAdd(size + c, 1u);
+        const int32_t a = pts[3 * v], b = pts[3 * v + 1], d = pts[3 * v + 2];
+        if (a < 0 || a > kFjMaxCoord || b < 0 || b > kFjMaxCoord || d < 0 || d > kFjMaxCoord) atomicAdd(bad, 1ull);
+    }
+}
+
+// points grouped by their component's rank (any order inside a group)
+__global__ void fj_scatter_kernel(const int32_t *__restrict__ comp, int64_t R, const int32_t *__restrict__ rank_of,
+                                  const unsigned *__restrict__ start, unsigned *__restrict__ fill,
+                                  int32_t *__restrict__ perm)
+{
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < R; v += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r = rank_of[comp[v]];
+        perm[start[r] + atomicAdd(fill + r, 1u)] = (int32_t)v;
+    }
+}
+
+struct FjChunk {
+    int32_t rank, begin, end;   // target positions [begin, end) of perm, all of one rank
+};
+
+// every query point q of a rank above the chunk's against the chunk's points:
+// key[chunk rank][q - qbase] = min over targets p of (d^2 << 32 | p)
+__global__ void __launch_bounds__(256) fj_nearest_kernel(const int32_t *__restrict__ pts,
+                                                         const int32_t *__restrict__ perm,
+                                                         const unsigned *__restrict__ start,
+                                                         const FjChunk *__restrict__ chunks, int64_t R, int64_t qbase,
+                                                         unsigned long long *__restrict__ key)
+{
+    __shared__ int4 tp[kFjChunk];
+    const FjChunk ch = chunks[blockIdx.x];
+    const int nt = ch.end - ch.begin;
+    for (int k = threadIdx.x; k < nt; k += blockDim.x) {
+        const int32_t p = perm[ch.begin + k];
+        tp[k] = make_int4(pts[3 * p], pts[3 * p + 1], pts[3 * p + 2], p);
+    }
+    __syncthreads();
+    const int64_t q0 = start[ch.rank + 1];
+    unsigned long long *krow = key + (int64_t)ch.rank * (R - qbase);
+    for (int64_t qi = q0 + threadIdx.x; qi < R; qi += blockDim.x) {
+        const int32_t q = perm[qi];
+        const int a = pts[3 * q], b = pts[3 * q + 1], c = pts[3 * q + 2];
+        unsigned long long best = ~0ull;
+        for (int k = 0; k < nt; ++k) {
+            const int4 t = tp[k];
+            const int da = t.x - a, db = t.y - b, dc = t.z - c;
+            const unsigned d2 = (unsigned)(da * da) + (unsigned)(db * db) + (unsigned)(dc * dc);
+            const unsigned long long kk = ((unsigned long long)d2 << 32) | (unsigned)t.w;
+            best = kk < best ? kk : best;
+        }
+        atomicMin(krow + (qi - qbase), best);
+    }
+}
+
+__global__ void fj_fill_kernel(unsigned long long *p, int64_t n)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        p[k] = ~0ull;
+}
+
+struct FjLayout {
+    size_t parent, root, par, pmin, cid, comp, size, rank, start, fill, perm, bcount, chunks, key, ctrl, total;
+    int64_t max_keys, max_chunks;
+};
+
+FjLayout fj_layout(int64_t R)
+{
+    FjLayout L{};
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align_up(off + bytes, 256);
+        return o;
+    };
+    const int64_t nb = div_up(R, kFjScanItems);
+    L.max_keys = 4 * R;
+    L.max_chunks = R / kFjChunk + R + 1;
+    L.parent = take(4 * (size_t)R);
+    L.root = take(4 * (size_t)R);
+    L.par = take((size_t)R);
+    L.pmin = take(4 * (size_t)R);
+    L.cid = take(4 * (size_t)R);
+    L.comp = take(4 * (size_t)R);
+    L.size = take(4 * (size_t)R);
+    L.rank = take(4 * (size_t)R);
+    L.start = take(4 * (size_t)(R + 1));
+    L.fill = take(4 * (size_t)R);
+    L.perm = take(4 * (size_t)R);
+    L.bcount = take(4 * (size_t)nb);
+    L.chunks = take(sizeof(FjChunk) * (size_t)L.max_chunks);
+    L.key = take(8 * (size_t)L.max_keys);
+    L.ctrl = take(32);
+    L.total = off;
+    return L;
+}
+
+}  // namespace
+}  // namespace m16
+
+extern "C" size_t m16_ridge_forest_joins_workspace_bytes(int64_t num_points)
+{
+    if (num_points < 1 || num_points > (int64_t)kIndexMask) return 0;
+    return fj_layout(num_points).total;
+}
+
+extern "C" int m16_ridge_forest_joins(const int32_t *pts3, int64_t num_points, const int32_t *edges_a,
+                                      const int32_t *edges_b, int64_t num_edges, int64_t max_pair_evaluations,
+                                      int32_t *join_a, int32_t *join_b, int64_t *num_joins, void *workspace,
+                                      size_t workspace_bytes, void *stream)
+{
+    const int64_t R = num_points;
+    if (R < 1 || R > (int64_t)kIndexMask || num_edges < 0 || num_edges >= R || !pts3 || !join_a || !join_b ||
+        !num_joins || (num_edges > 0 && (!edges_a || !edges_b)))
+        return M16_ERR_BAD_ARG;
+    const FjLayout Ly = fj_layout(R);
+    if (!workspace || workspace_bytes < Ly.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;
+    *num_joins = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *ws = (char *)workspace;
+    uint32_t *parent = (uint32_t *)(ws + Ly.parent);
+    uint32_t *root = (uint32_t *)(ws + Ly.root);
+    uint8_t *par = (uint8_t *)(ws + Ly.par);
+    int32_t *pmin = (int32_t *)(ws + Ly.pmin);
+    int32_t *cid = (int32_t *)(ws + Ly.cid);
+    int32_t *comp = (int32_t *)(ws + Ly.comp);
+    unsigned *size = (unsigned *)(ws + Ly.size);
+    int32_t *rank_of = (int32_t *)(ws + Ly.rank);
+    unsigned *start = (unsigned *)(ws + Ly.start);
+    unsigned *fill = (unsigned *)(ws + Ly.fill);
+    int32_t *perm = (int32_t *)(ws + Ly.perm);
+    unsigned *bcount = (unsigned *)(ws + Ly.bcount);
+    FjChunk *chunks = (FjChunk *)(ws + Ly.chunks);
+    unsigned long long *key = (unsigned long long *)(ws + Ly.key);
+    unsigned long long *ctrl = (unsigned long long *)(ws + Ly.ctrl);   // [0] walks at the limit, [1] bad edges, [2] bad coordinates
+    const int gr = rs_grid(R), ge = rs_grid(std::max<int64_t>(num_edges, 1));
+    const int64_t nb = div_up(R, kFjScanItems);
+    // components of the forest: union-find, each root its component's lowest point
+    M16_CUDA_TRY(cudaMemsetAsync(ctrl, 0, 32, st));
+    M16_CUDA_TRY(cudaMemsetAsync(pmin, 0x7f, 4 * (size_t)R, st));
+    rs_init_kernel<<<gr, kRsBlock, 0, st>>>(parent, R);
+    if (num_edges > 0)
+        rs_union_kernel<<<ge, kRsBlock, 0, st>>>(edges_a, edges_b, nullptr, num_edges, R, parent, ctrl, ctrl + 1);
+    rs_flatten_kernel<<<gr, kRsBlock, 0, st>>>(parent, R, root, par, pmin, ctrl);
+    fj_root_count_kernel<<<(unsigned)nb, 256, 0, st>>>(root, R, bcount);
+    M16_CUDA_TRY(cudaGetLastError());
+    std::vector<unsigned> hb(nb);
+    M16_CUDA_TRY(cudaMemcpyAsync(hb.data(), bcount, 4 * (size_t)nb, cudaMemcpyDeviceToHost, st));
+    M16_CUDA_TRY(cudaStreamSynchronize(st));
+    unsigned C = 0;
+    for (int64_t b = 0; b < nb; ++b) {
+        const unsigned c = hb[b];
+        hb[b] = C;
+        C += c;
+    }
+    if (C <= 1) return M16_OK;   // one tree already
+    M16_CUDA_TRY(cudaMemcpyAsync(bcount, hb.data(), 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
+    fj_root_id_kernel<<<(unsigned)nb, 256, 0, st>>>(root, R, bcount, cid);
+    M16_CUDA_TRY(cudaMemsetAsync(size, 0, 4 * (size_t)C, st));
+    fj_comp_kernel<<<gr, kRsBlock, 0, st>>>(root, cid, pts3, R, comp, size, ctrl + 2);
+    M16_CUDA_TRY(cudaGetLastError());
+    std::vector<unsigned> hsize(C);
+    unsigned long long hc[3];
+    M16_CUDA_TRY(cudaMemcpyAsync(hsize.data(), size, 4 * (size_t)C, cudaMemcpyDeviceToHost, st));
+    M16_CUDA_TRY(cudaMemcpyAsync(hc, ctrl, 24, cudaMemcpyDeviceToHost, st));
+    M16_CUDA_TRY(cudaStreamSynchronize(st));
+    if (hc[1] != 0 || hc[2] != 0) return M16_ERR_BAD_ARG;
+    if (hc[0] != 0) return M16_ERR_TIMEOUT;
+    // ranks: components by size, largest first (ties by number)
+    std::vector<int32_t> order(C), rank_h(C);
+    for (unsigned c = 0; c < C; ++c) order[c] = (int32_t)c;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return hsize[a] > hsize[b]; });
+    std::vector<unsigned> hstart(C + 1, 0);
+    for (unsigned t = 0; t < C; ++t) {
+        rank_h[order[t]] = (int32_t)t;
+        hstart[t + 1] = hstart[t] + hsize[order[t]];
+    }
+    // the work and memory of the search: every rank against the ranks after it
+    const int64_t qbase = hstart[1];
+    double work = 0.0;
+    std::vector<FjChunk> hch;
+    for (unsigned t = 0; t + 1 < C; ++t) {
+        work += (double)hsize[order[t]] * (double)(R - hstart[t + 1]);
+        for (int64_t b0 = hstart[t]; b0 < (int64_t)hstart[t + 1]; b0 += kFjChunk)
+            hch.push_back(FjChunk{(int32_t)t, (int32_t)b0, (int32_t)std::min<int64_t>(b0 + kFjChunk, hstart[t + 1])});
+    }
+    const int64_t nkeys = (int64_t)(C - 1) * (R - qbase);
+    if (work > (double)max_pair_evaluations || nkeys > Ly.max_keys || (int64_t)hch.size() > Ly.max_chunks ||
+        (int64_t)hch.size() > INT32_MAX)
+        return M16_ERR_TOO_LARGE;
+    M16_CUDA_TRY(cudaMemcpyAsync(rank_of, rank_h.data(), 4 * (size_t)C, cudaMemcpyHostToDevice, st));
+    M16_CUDA_TRY(cudaMemcpyAsync(start, hstart.data(), 4 * (size_t)(C + 1), cudaMemcpyHostToDevice, st));
+    M16_CUDA_TRY(cudaMemcpyAsync(chunks, hch.data(), sizeof(FjChunk) * hch.size(), cudaMemcpyHostToDevice, st));
+    M16_CUDA_TRY(cudaMemsetAsync(fill, 0, 4 * (size_t)C, st));
+    fj_scatter_kernel<<<gr, kRsBlock, 0, st>>>(comp, R, rank_of, start, fill, perm);
+    fj_fill_kernel<<<rs_grid(nkeys), kRsBlock, 0, st>>>(key, nkeys);
+    fj_nearest_kernel<<<(unsigned)hch.size(), 256, 0, st>>>(pts3, perm, start, chunks, R, qbase, key);
+    M16_CUDA_TRY(cudaGetLastError());
+    std::vector<unsigned long long> hkey(nkeys);
+    std::vector<int32_t> hperm(R - qbase);
+    M16_CUDA_TRY(cudaMemcpyAsync(hkey.data(), key, 8 * (size_t)nkeys, cudaMemcpyDeviceToHost, st));
+    M16_CUDA_TRY(cudaMemcpyAsync(hperm.data(), perm + qbase, 4 * (size_t)(R - qbase), cudaMemcpyDeviceToHost, st));
+    M16_CUDA_TRY(cudaStreamSynchronize(st));
+    // least (d^2, lo, hi) of every pair of ranks (s > t)
+    struct Cand {
+        uint64_t d2;
+        int32_t lo, hi, s, t;
+    };
+    std::vector<Cand> cand;
+    cand.reserve((size_t)C * (C - 1) / 2);
+    for (unsigned t = 0; t + 1 < C; ++t) {
+        const unsigned long long *krow = hkey.data() + (int64_t)t * (R - qbase);
+        for (unsigned s = t + 1; s < C; ++s) {
+            Cand best{~0ull, INT32_MAX, INT32_MAX, (int32_t)s, (int32_t)t};
+            for (int64_t qi = hstart[s]; qi < (int64_t)hstart[s + 1]; ++qi) {
+                const unsigned long long k = krow[qi - qbase];
+                const int32_t q = hperm[qi - qbase], p = (int32_t)(k & 0xffffffffu);
+                const uint64_t d2 = k >> 32;
+                const int32_t lo = std::min(q, p), hi = std::max(q, p);
+                if (d2 < best.d2 || (d2 == best.d2 && (lo < best.lo || (lo == best.lo && hi < best.hi))))
+                    best = Cand{d2, lo, hi, (int32_t)s, (int32_t)t};
+            }
+            cand.push_back(best);
+        }
+    }
+    // Kruskal over the components in (weight, lo, hi) order
+    std::sort(cand.begin(), cand.end(), [](const Cand &a, const Cand &b) {
+        if (a.d2 != b.d2) return a.d2 < b.d2;
+        if (a.lo != b.lo) return a.lo < b.lo;
+        return a.hi < b.hi;
+    });
+    std::vector<int32_t> uf(C);
+    for (unsigned c = 0; c < C; ++c) uf[c] = (int32_t)c;
+    auto find = [&](int32_t x) {
+        while (uf[x] != x) {
+            uf[x] = uf[uf[x]];
+            x = uf[x];
+        }
+        return x;
+    };
+    int64_t nj = 0;
+    for (const Cand &c : cand) {
+        const int32_t a = find(c.s), b = find(c.t);
+        if (a == b) continue;
+        uf[std::max(a, b)] = std::min(a, b);
+        join_a[nj] = c.lo;
+        join_b[nj] = c.hi;
+        if (++nj == (int64_t)C - 1) break;
+    }
+    *num_joins = nj;
     return M16_OK;
 }

@@ -98,9 +98,10 @@ def _local_mst_host(pts, vs, r, offsets):
     return _kruskal_by_order(R, i, j, (j, i, w))
 
 
-def _local_mst_gpu(pts, vs, r, offsets):
+def _local_mst_gpu(pts, vs, r, offsets, keep_device=False):
     """The local phase on the GPU (m16_ridge_mst_local, Boruvka rounds in the
-    same (weight, i, j) order): the same edge set as _local_mst_host."""
+    same (weight, i, j) order): the same edge set as _local_mst_host.  With
+    keep_device, also the device points (int32 R x 3) and edges (int32 E x 2)."""
     torch = N.torch_mod()
     L = N.lib()
     R = len(pts)
@@ -118,7 +119,36 @@ def _local_mst_gpu(pts, vs, r, offsets):
                                N.stream_ptr())
     N.check("m16_ridge_mst_local", st)
     e = edges[:ne.value].cpu().numpy().astype(np.int64)
+    if keep_device:
+        return e[:, 0], e[:, 1], d_pts, edges[:ne.value]
     return e[:, 0], e[:, 1]
+
+
+# pair evaluations above which the joins stay on the host (k-d trees)
+JOIN_MAX_PAIR_EVALUATIONS = 40_000_000_000
+
+
+def _joins_gpu(d_pts, d_edges):
+    """The joins of the local trees on the device (m16_ridge_forest_joins) for
+    unit voxel size: (a, b) host arrays of the joining edges, or None where
+    the exact search would take more than JOIN_MAX_PAIR_EVALUATIONS distance
+    evaluations (then the host joins them)."""
+    L = N.lib()
+    R = int(d_pts.shape[0])
+    ea = d_edges[:, 0].contiguous()
+    eb = d_edges[:, 1].contiguous()
+    ja = np.empty(max(R - 1, 1), np.int32)
+    jb = np.empty(max(R - 1, 1), np.int32)
+    nj = ctypes.c_int64(0)
+    ws = N.workspace(L.m16_ridge_forest_joins_workspace_bytes(R))
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    st = L.m16_ridge_forest_joins(N.ptr(d_pts), R, N.ptr(ea), N.ptr(eb), int(ea.numel()),
+                                  JOIN_MAX_PAIR_EVALUATIONS, vp(ja), vp(jb), ctypes.byref(nj), N.ptr(ws), ws.numel(),
+                                  N.stream_ptr())
+    if st == N.M16_ERR_TOO_LARGE:
+        return None
+    N.check("m16_ridge_forest_joins", st)
+    return ja[:nj.value].astype(np.int64), jb[:nj.value].astype(np.int64)
 
 
 def forest_components(n, ea, eb):
@@ -140,14 +170,17 @@ def forest_components(n, ea, eb):
     return int(np.count_nonzero(starts)), comp
 
 
-def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, local="gpu"):
+def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, local="gpu", joins_on_device=True):
     """Edges (a, b) of the (weight, i, j)-ordered Euclidean MST of integer
     points (R x 3, axis order 0, 1, 2, distinct) with per-axis voxel size.
     With join_components=False only the local phase runs: the result is the
     MST minus its edges longer than r, i.e. a spanning tree of every group of
     points linked by steps not longer than r (each 26-connected set lies in
     one such group).  local selects where the local phase runs ("gpu", the
-    default, or "host"); both give the same edges."""
+    default, or "host"); both give the same edges.  With the local phase on
+    the GPU and unit voxel size, the trees are joined on the device too
+    (m16_ridge_forest_joins, exact in integer arithmetic) unless
+    joins_on_device is False; otherwise k-d trees on the host join them."""
     pts = np.asarray(points, dtype=np.int64)
     R = len(pts)
     if R < 2:
@@ -155,8 +188,10 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, lo
     vs = np.asarray(np.multiply(np.ones(3), voxel_size), np.float64)
     u = np.multiply(pts, vs)   # the coordinates pdist sees
     r, offsets = _local_offsets(vs)
+    device = None
     if local == "gpu":
-        ta, tb = _local_mst_gpu(pts, vs, r, offsets)
+        ta, tb, d_pts, d_edges = _local_mst_gpu(pts, vs, r, offsets, keep_device=True)
+        device = (d_pts, d_edges)
     elif local == "host":
         ta, tb = _local_mst_host(pts, vs, r, offsets)
     else:
@@ -164,6 +199,10 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, lo
     # global phase: join the local trees
     if not join_components or len(ta) == R - 1:   # not asked for, or already one tree
         return ta, tb
+    if device is not None and np.all(vs == 1.0) and joins_on_device:
+        j = _joins_gpu(*device)
+        if j is not None:
+            return np.concatenate([ta, j[0]]), np.concatenate([tb, j[1]])
     ncomp, comp = forest_components(R, ta, tb)
     by_comp = np.argsort(comp, kind="stable")   # each component's points in index order
     members = np.split(by_comp, np.cumsum(np.bincount(comp, minlength=ncomp))[:-1])

@@ -114,3 +114,70 @@ def test_duplicate_or_outside_points_are_rejected():
     assert ok == (N.M16_OK, 2)
     assert call([[0, 0, 0], [0, 0, 1], [0, 0, 1]], (0, 0, 0), (1, 1, 2))[0] == N.M16_ERR_BAD_ARG
     assert call([[0, 0, 0], [0, 0, 5]], (0, 0, 0), (1, 1, 2))[0] == N.M16_ERR_BAD_ARG
+
+
+def _segments(rng, n_seg, big):
+    """A ridge-like point set: one long thick curve and many short specks,
+    far apart, with equal distances everywhere (integer points)."""
+    t = np.linspace(0, 6 * np.pi, big)
+    curve = np.stack([t * 6, 80 + 50 * np.sin(t), 80 + 50 * np.cos(t)], -1)
+    pts = [np.round(curve[:, None, :] + rng.randint(-1, 2, (big, 3, 3))).reshape(-1, 3)]
+    for _ in range(n_seg):
+        c = rng.randint(5, 150, 3)
+        pts.append(c + np.cumsum(rng.randint(-1, 2, (rng.randint(1, 40), 3)), axis=0))
+    pts = np.unique(np.concatenate(pts), axis=0)
+    pts = pts[pts.min(1) >= 0].astype(np.int64)
+    return pts[rng.permutation(len(pts))]
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_device_joins_equal_the_host_joins(seed):
+    """m16_ridge_forest_joins (the global phase on the device) gives the edge
+    set of the k-d tree joins on the host, and of the oracle's stable Kruskal
+    where that fits."""
+    from miccai2016_gb300.ridge_mst import ridge_mst_edges
+    rng = np.random.RandomState(30 + seed)
+    pts = _segments(rng, 10 + 10 * seed, 600 + 400 * seed)
+    a, b = ridge_mst_edges(pts, (1, 1, 1), local="gpu")
+    h = ridge_mst_edges(pts, (1, 1, 1), local="gpu", joins_on_device=False)
+    assert len(a) == len(pts) - 1
+    assert _set(a, b) == _set(*h)
+    if seed == 0:
+        t = A.prim_mst(pts, (1, 1, 1)).tocoo()
+        assert _set(a, b) == _set(t.row, t.col)
+
+
+def test_device_joins_on_clusters_full_of_ties():
+    from miccai2016_gb300.ridge_mst import ridge_mst_edges
+    rng = np.random.RandomState(5)
+    for _ in range(3):
+        pts = np.unique(np.concatenate([rng.randint(0, 6, (40, 3)) * 3 + rng.randint(0, 60, 3)
+                                        for _ in range(12)]), axis=0)
+        pts = pts[rng.permutation(len(pts))].astype(np.int64)
+        a, b = ridge_mst_edges(pts, (1, 1, 1), local="gpu")
+        t = A.stable_mst(pts, (1, 1, 1)).tocoo()
+        assert _set(a, b) == _set(t.row, t.col)
+
+
+def test_device_joins_reject_and_decline():
+    import torch
+    from miccai2016_gb300 import _native as N
+    L = N.lib()
+    pts = torch.tensor([[0, 0, 0], [0, 0, 9], [40000, 0, 0]], dtype=torch.int32, device="cuda")
+    e = torch.zeros((0, 2), dtype=torch.int32, device="cuda")
+    ja, jb = np.zeros(2, np.int32), np.zeros(2, np.int32)
+    nj = ctypes.c_int64(0)
+    ws = N.workspace(L.m16_ridge_forest_joins_workspace_bytes(3))
+    vp = lambda x: x.ctypes.data_as(ctypes.c_void_p)
+    ea, eb = e[:, 0].contiguous(), e[:, 1].contiguous()
+    # a coordinate beyond 32767: rejected
+    assert L.m16_ridge_forest_joins(N.ptr(pts), 3, N.ptr(ea), N.ptr(eb), 0, 10 ** 9, vp(ja), vp(jb),
+                                    ctypes.byref(nj), N.ptr(ws), ws.numel(), N.stream_ptr()) == N.M16_ERR_BAD_ARG
+    pts[2, 0] = 7
+    # a budget too small for the search: declined, nothing written
+    assert L.m16_ridge_forest_joins(N.ptr(pts), 3, N.ptr(ea), N.ptr(eb), 0, 1, vp(ja), vp(jb),
+                                    ctypes.byref(nj), N.ptr(ws), ws.numel(), N.stream_ptr()) == N.M16_ERR_TOO_LARGE
+    assert nj.value == 0
+    assert L.m16_ridge_forest_joins(N.ptr(pts), 3, N.ptr(ea), N.ptr(eb), 0, 10 ** 9, vp(ja), vp(jb),
+                                    ctypes.byref(nj), N.ptr(ws), ws.numel(), N.stream_ptr()) == N.M16_OK
+    assert nj.value == 2 and _set(ja[:2], jb[:2]) == {(0, 2), (0, 1)}
