@@ -12,8 +12,7 @@ iterations (residual checked every 30).  One step = one solve.
          pinned host inputs: H2D of the inputs and D2H of u inside every step
   roofline  the flow sweep (the dominant kernel of an iteration: flow 44 B,
          labels 40 B per voxel), its launch time measured with CUDA events on
-         the solve's stream in a second pass over the same solves; the fused
-         one-launch iteration (84 B per voxel) is timed once beside it
+         the solve's stream in a second pass over the same solves
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun every rank runs its own replica (the solves are independent).
@@ -326,10 +325,6 @@ def run_ours(args, cfg):
         s = N.SolveStats(1, 0, 0, 0, 0.0, 0.0, N.PATH_DEFAULT, 0)
         solve(s)
         p_ms += s.p_ms; u_ms += s.u_ms; p_n += s.p_launches; u_n += s.u_launches
-    # and once with the fused iteration (one launch per iteration) for comparison
-    s2 = N.SolveStats(1, 0, 0, 0, 0.0, 0.0, N.PATH_FUSED, 0)
-    solve(s2)
-    fused_ms, fused_n = s2.p_ms, s2.p_launches
     torch.cuda.synchronize()
     clocks = sampler.stop() if sampler else None
     if dist:
@@ -371,8 +366,6 @@ def run_ours(args, cfg):
             dist.destroy_process_group()
         return
     peak, peak_kind = _peaks()
-    f_avg = fused_ms / max(fused_n, 1)
-    f_gbs = F_BYTES * n / (f_avg * 1e-3) / 1e9
     p_avg = p_ms / max(p_n, 1)
     u_avg = u_ms / max(u_n, 1)
     p_gbs = P_BYTES * n / (p_avg * 1e-3) / 1e9
@@ -400,9 +393,7 @@ def run_ours(args, cfg):
                "iteration_in_solve": {"ms": ms_per_step / cfg["num_iter"],
                                       "GB/s": F_BYTES * n / (ms_per_step / cfg["num_iter"] * 1e-3) / 1e9,
                                       "frac": F_BYTES * n / (ms_per_step / cfg["num_iter"] * 1e-3) / 1e9 / peak,
-                                      "bytes_per_voxel": F_BYTES},
-               "fused_path": {"mf_fused_kernel_avg_ms": f_avg, "launches": fused_n, "GB/s": f_gbs,
-                              "frac": f_gbs / peak, "bytes_per_voxel": F_BYTES}}
+                                      "bytes_per_voxel": F_BYTES}}
     cpu_v, kind, cpu_dt, sample = cpu_baseline(cfg, inp, iters=args.cpu_iters) if rank == 0 else (
         None, None, None, None)
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -897,10 +888,10 @@ def run_stages(args, cfg):
 
 
 def run_paths(args, cfg):
-    """The iteration paths of the single solve side by side on one workload:
-    two sweeps, the fused iteration and two iterations per launch (at the
-    default z-chunk and at those of --pair-zc), CUDA events around whole
-    solves and, in a second pass, around every launch.  Prints one JSON line."""
+    """The single solve's launches on one workload: the two sweeps with
+    programmatic dependent launch (the default) and in plain stream order,
+    CUDA events around whole solves and, in a second pass, around every
+    launch.  Prints one JSON line."""
     import torch
     torch.cuda.set_device(0)
     from miccai2016_gb300 import _native as N
@@ -917,9 +908,8 @@ def run_paths(args, cfg):
     sq = (ctypes.c_double * 3)(*np.sqrt(P.ATV_EIGS).tolist())
     stream = torch.cuda.current_stream()
 
-    def solve(path, zc=0, timing=0, flags=0):
-        s = N.SolveStats(timing, 0, 0, 0, 0.0, 0.0, path, flags)
-        s.pair_zc = zc
+    def solve(timing=0, flags=0):
+        s = N.SolveStats(timing, 0, 0, 0, 0.0, 0.0, N.PATH_DEFAULT, flags)
         it = ctypes.c_int32(0)
         st = L.m16_maxflow_solve_ex(N.ptr(d["img"]), N.ptr(d["quats"]), sq, None, N.ptr(d["alpha"]), 0.0,
                                     N.ptr(d["cs"]), N.ptr(d["ct"]), None, shape[0], shape[1], shape[2],
@@ -928,46 +918,26 @@ def run_paths(args, cfg):
         N.check("m16_maxflow_solve_ex", st)
         return s
 
-    def timed(path, zc=0, flags=0):
+    def timed(flags=0):
         for _ in range(args.warmup):
-            solve(path, zc, flags=flags)
+            solve(flags=flags)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            s = solve(path, zc, flags=flags)
+            s = solve(flags=flags)
         e1.record(stream)
         torch.cuda.synchronize()
-        k = solve(path, zc, timing=1, flags=flags)
-        r = dict(ms_per_solve=e0.elapsed_time(e1) / args.steps, launches=s.launches,
-                 iterations_not_in_pairs=k.p_launches)
-        if path == N.PATH_PAIRS:
-            r.update(pair_launches=k.pair_launches, pair_zc=k.pair_zc,
-                     pair_launch_ms=k.pair_ms / max(k.pair_launches, 1))
-        if path == N.PATH_FUSED:
-            r.update(fused_launch_ms=k.p_ms / max(k.p_launches, 1))
-        elif k.u_launches > 0:
-            r.update(flow_sweep_ms=k.p_ms / max(k.p_launches, 1), label_sweep_ms=k.u_ms / max(k.u_launches, 1))
-        return r
+        k = solve(timing=1, flags=flags)
+        return dict(ms_per_solve=e0.elapsed_time(e1) / args.steps, launches=s.launches,
+                    flow_sweep_ms=k.p_ms / max(k.p_launches, 1), label_sweep_ms=k.u_ms / max(k.u_launches, 1))
 
-    wanted = set(args.paths.split(","))
-    out = {}
-    u_ref = None
-    if "two_sweeps" in wanted:
-        out["two_sweeps"] = timed(N.PATH_TWO_SWEEPS)
-        u_ref = u.clone()
-        out["two_sweeps_no_pdl"] = timed(N.PATH_TWO_SWEEPS, flags=N.SOLVE_NO_PDL)
-        out["two_sweeps_no_pdl"]["max_u_diff_vs_pdl"] = float((u - u_ref).abs().max())
-    if "fused" in wanted:
-        out["fused"] = timed(N.PATH_FUSED)
-    if "pairs" in wanted:
-        out["pairs"] = timed(N.PATH_PAIRS)
-        if u_ref is not None:
-            out["pairs"]["max_u_diff_vs_two_sweeps"] = float((u - u_ref).abs().max())
-        for zc in [int(v) for v in args.pair_zc.split(",") if v]:
-            out["pairs_zc%d" % zc] = timed(N.PATH_PAIRS, zc)
-    print(json.dumps({"workload": "iteration paths of one %s solve, %d iterations" % ("x".join(map(str, shape)),
-                                                                                       cfg["num_iter"]),
+    out = {"two_sweeps": timed()}
+    u_ref = u.clone()
+    out["two_sweeps_no_pdl"] = timed(flags=N.SOLVE_NO_PDL)
+    out["two_sweeps_no_pdl"]["max_u_diff_vs_pdl"] = float((u - u_ref).abs().max())
+    print(json.dumps({"workload": "launches of one %s solve, %d iterations" % ("x".join(map(str, shape)),
+                                                                                cfg["num_iter"]),
                       "steps": args.steps, "warmup": args.warmup, "paths": out}))
 
 
@@ -998,10 +968,6 @@ def main():
                     help="serving comparison: requests of the saturated run (all at t = 0; 0 skips it)")
     ap.add_argument("--cpu-iters", type=int, default=100,
                     help="iterations of the CPU-baseline sample of the default arm")
-    ap.add_argument("--paths", default="two_sweeps,fused,pairs",
-                    help="paths workloads: which iteration paths to time")
-    ap.add_argument("--pair-zc", default="",
-                    help="paths workloads: comma-separated z-chunks of the two-iteration launches to time too")
     args = ap.parse_args()
     if args.workload.startswith("paths"):
         run_paths(args, _workload("plain" + args.workload[len("paths"):]))

@@ -91,19 +91,13 @@ int m16_maxflow_solve(const float *img, const float *quat3, const double *sqeval
                       float *u, int32_t *iterations, double *residuals, int32_t residuals_cap,
                       int32_t *n_residuals, void *workspace, size_t workspace_bytes, void *stream);
 
-/* Iteration paths of the single solve.  TWO_SWEEPS: a flow launch, then a
- * label launch; FUSED: one launch per iteration (flow and labels of a 32 x 8
- * x z tile together, the flow field and tmp double-buffered); PAIRS: two
- * iterations per launch (a 28 x 12 x z tile with a two-voxel halo, the state
- * double-buffered between launches) wherever no residual check falls on the
- * first of the two, the other iterations as two sweeps -- with per-voxel
- * eigenvalues PAIRS runs as TWO_SWEEPS.  All do the same per-voxel
- * arithmetic; DEFAULT is the one measured fastest on sm_103a.  The workspace
- * size reported by m16_maxflow_workspace_bytes covers every path. */
+/* Iteration paths of the single solve: a flow launch, then a label launch
+ * per iteration (DEFAULT and TWO_SWEEPS are the same path).  The values 2
+ * and 3 (one launch per iteration; two iterations per launch) were measured
+ * slower than the two sweeps at every volume size on sm_103a and were
+ * removed: they return M16_ERR_BAD_ARG. */
 #define M16_PATH_DEFAULT 0
 #define M16_PATH_TWO_SWEEPS 1
-#define M16_PATH_FUSED 2
-#define M16_PATH_PAIRS 3
 
 /* Counters of one solve, for benchmarks and tracing. */
 typedef struct m16_solve_stats {
@@ -111,18 +105,15 @@ typedef struct m16_solve_stats {
     int32_t launches;      /* out: kernels the call launched */
     int32_t p_launches;    /* out: flow (P) kernel launches that ran */
     int32_t u_launches;    /* out: label (U) kernel launches that ran */
-    double p_ms;           /* out: summed device time of the P launches, or of the fused
-                              iteration launches (time_kernels only) */
+    double p_ms;           /* out: summed device time of the P launches (time_kernels only) */
     double u_ms;           /* out: summed device time of the U launches (time_kernels only) */
     int32_t path;          /* in: M16_PATH_* -- how an iteration is launched */
     int32_t flags;         /* in: M16_BATCH_* options of m16_batch_solve (0 elsewhere) */
     int32_t blocks_per_sm; /* out (m16_batch_solve): the sweeps' tile shape in use at the end, as the
                               target blocks per SM its z-chunk was chosen for */
-    int32_t pair_launches; /* out: two-iteration launches that ran (M16_PATH_PAIRS); p_launches and
-                              u_launches then count the iterations run as two sweeps */
-    double pair_ms;        /* out: summed device time of the two-iteration launches (time_kernels only) */
-    int32_t pair_zc;       /* in: z-planes per block of the two-iteration launches, 0 = the default;
-                              out: the value used (0 on other paths) */
+    int32_t pair_launches; /* reserved (0): kept for the layout of ABI versions 3 and 4 */
+    double pair_ms;        /* reserved (0) */
+    int32_t pair_zc;       /* reserved (0) */
     int32_t reserved;
 } m16_solve_stats;
 

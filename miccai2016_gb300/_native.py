@@ -50,8 +50,8 @@ class CutParams(ctypes.Structure):
                 ("update", _i32), ("scaling", _f64 * 3)]
 
 
-# iteration paths of the single solve (m16_solve_stats.path)
-PATH_DEFAULT, PATH_TWO_SWEEPS, PATH_FUSED, PATH_PAIRS = 0, 1, 2, 3
+# iteration paths of the single solve (m16_solve_stats.path): both the two sweeps
+PATH_DEFAULT, PATH_TWO_SWEEPS = 0, 1
 
 
 BATCH_NO_GRAPH = 1   # m16_solve_stats.flags

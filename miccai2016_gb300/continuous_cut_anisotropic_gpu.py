@@ -53,12 +53,8 @@ class CmfCutQAnisotropicGpu(TreePrintable):
         self.last_iterations = None
         self.last_residuals = None
         self._ws = None
-        # how an iteration is launched (N.PATH_DEFAULT, PATH_TWO_SWEEPS,
-        # PATH_FUSED or PATH_PAIRS); the paths give the same result within
-        # float rounding
+        # how an iteration is launched (N.PATH_DEFAULT = N.PATH_TWO_SWEEPS)
         self.iteration_path = N.PATH_DEFAULT
-        # z-planes per block of the two-iteration launches (0: the library's choice)
-        self.pair_zc = 0
         self.last_stats = None
 
     # -- reference: execute() with its exception-forwarding wrapper (:143-196)
@@ -132,7 +128,6 @@ class CmfCutQAnisotropicGpu(TreePrintable):
         iters = ctypes.c_int32(0)
         nres = ctypes.c_int32(0)
         stats = N.SolveStats(0, 0, 0, 0, 0.0, 0.0, int(self.iteration_path), 0)
-        stats.pair_zc = int(self.pair_zc)
         st = L.m16_maxflow_solve_ex(N.ptr(d_img), N.ptr(d_q), sqc, N.ptr(sqp), N.ptr(d_alpha), alpha_scalar,
                                     N.ptr(d_cs), N.ptr(d_ct), N.ptr(d_lab), shape[0], shape[1], shape[2],
                                     ctypes.byref(cp), N.ptr(u), ctypes.byref(iters), resid, cap,

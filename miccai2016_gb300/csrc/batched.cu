@@ -391,7 +391,7 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
 {
     if (!params || params->update < 1 || params->num_iter < 0 || !(params->cc > 0.0)) return M16_ERR_BAD_ARG;
     if (!batch_args_ok(vols, nvol, inst, ninst)) return M16_ERR_BAD_ARG;
-    if (stats && (stats->path < M16_PATH_DEFAULT || stats->path > M16_PATH_FUSED)) return M16_ERR_BAD_ARG;
+    if (stats && stats->path != M16_PATH_DEFAULT && stats->path != M16_PATH_TWO_SWEEPS) return M16_ERR_BAD_ARG;
     const Plan P = make_plan(nvol, inst, ninst);
     const BatchLayout L = batch_layout(vols, nvol, inst, ninst, P);
     if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;

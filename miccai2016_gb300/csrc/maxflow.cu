@@ -27,8 +27,6 @@
 
 #include "common.cuh"
 #include "sweeps.cuh"
-#include "fused.cuh"
-#include "pairs.cuh"
 
 namespace m16 {
 namespace {
@@ -48,8 +46,6 @@ struct MfArgs {
     float sq0, sq1, sq2, isq0, isq1, isq2;
     float alpha_scalar;
     float *hp0, *hp1, *hp2, *tmp, *pt, *u;
-    float *hpB0, *hpB1, *hpB2, *tmpB;   // second ping-pong set of the fused iteration
-    float *ptB, *uB;                    // with hpB, tmpB: the second state set of the pair kernel
     const float4 *q4;
     const float *alpha, *sqeigs, *cs, *ct;
     const uint8_t *labels;
@@ -127,10 +123,6 @@ __global__ void mf_init_kernel(MfArgs a, const float *__restrict__ img, const fl
 #ifndef M16_MF_MINB
 #define M16_MF_MINB 4
 #endif
-// resident blocks per SM the fused kernel is compiled for (3 caps it at 64 registers)
-#ifndef M16_MF_FUSED_MINB
-#define M16_MF_FUSED_MINB 3
-#endif
 constexpr int kZB = kMfZB > kMfUZB ? kMfZB : kMfUZB;   // z-chunks are whole load batches of both sweeps
 
 __device__ __forceinline__ FlowView flow_view(const MfArgs &a)
@@ -188,126 +180,6 @@ __global__ void __launch_bounds__(kBX * kBY, M16_MF_MINB) mf_update_u_kernel(MfA
     }
 }
 
-// ---- the fused iteration (fused.cuh): P and U in one launch ---------------------
-// parity 0 reads (hp, tmp) and writes (hpB, tmpB); parity 1 the other way round.
-template <bool POINTWISE, bool ALPHA_ARR, bool SUPERVISED, bool CHECK>
-__global__ void __launch_bounds__(kFX * kFY, M16_MF_FUSED_MINB) mf_fused_kernel(MfArgs a, int parity)
-{
-    __shared__ float sm[2][2][kFY][kFX];
-    __shared__ float vals[kFX * kFY];
-    if (__ldcg(&a.ctrl->stopped)) return;
-    FusedView f;
-    f.d0 = a.d0; f.d1 = a.d1; f.d2 = a.d2;
-    f.ss0 = a.ss0; f.ss1 = a.ss1; f.ss2 = a.ss2; f.rcc = a.rcc; f.rs0 = a.rs0; f.rs1 = a.rs1; f.rs2 = a.rs2;
-    f.sq0 = a.sq0; f.sq1 = a.sq1; f.sq2 = a.sq2; f.isq0 = a.isq0; f.isq1 = a.isq1; f.isq2 = a.isq2;
-    f.alpha_scalar = a.alpha_scalar; f.alpha = a.alpha; f.grad2 = nullptr; f.w = 0.f; f.neg_inv_decay2 = 0.f;
-    f.exp_alpha = 0;
-    f.sqeigs = a.sqeigs; f.q4 = a.q4;
-    if (parity == 0) {
-        f.tmp_in = a.tmp; f.hp0_in = a.hp0; f.hp1_in = a.hp1; f.hp2_in = a.hp2;
-        f.tmp_out = a.tmpB; f.hp0_out = a.hpB0; f.hp1_out = a.hpB1; f.hp2_out = a.hpB2;
-    } else {
-        f.tmp_in = a.tmpB; f.hp0_in = a.hpB0; f.hp1_in = a.hpB1; f.hp2_in = a.hpB2;
-        f.tmp_out = a.tmp; f.hp0_out = a.hp0; f.hp1_out = a.hp1; f.hp2_out = a.hp2;
-    }
-    f.cs = a.cs; f.ct = a.ct; f.labels = a.labels; f.pt = a.pt; f.u = a.u;
-    const int z0 = blockIdx.z * a.zc;
-    const float acc = fused_tile<POINTWISE, ALPHA_ARR ? kAlphaArray : kAlphaScalar, SUPERVISED>(
-        f, blockIdx.x, blockIdx.y, z0, min(z0 + a.zc, a.d0), sm);
-    if (CHECK) {
-        const float s = fused_block_sum(acc, vals);
-        if (threadIdx.x == 0 && threadIdx.y == 0)
-            a.partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
-    }
-}
-
-template <bool CHECK>
-void launch_fused(bool pointwise, bool alpha_arr, bool sup, dim3 grid, cudaStream_t st, const MfArgs &a, int parity)
-{
-    const dim3 block(kFX, kFY, 1);
-    if (pointwise) {
-        if (alpha_arr) {
-            if (sup) mf_fused_kernel<true, true, true, CHECK><<<grid, block, 0, st>>>(a, parity);
-            else mf_fused_kernel<true, true, false, CHECK><<<grid, block, 0, st>>>(a, parity);
-        } else {
-            if (sup) mf_fused_kernel<true, false, true, CHECK><<<grid, block, 0, st>>>(a, parity);
-            else mf_fused_kernel<true, false, false, CHECK><<<grid, block, 0, st>>>(a, parity);
-        }
-    } else {
-        if (alpha_arr) {
-            if (sup) mf_fused_kernel<false, true, true, CHECK><<<grid, block, 0, st>>>(a, parity);
-            else mf_fused_kernel<false, true, false, CHECK><<<grid, block, 0, st>>>(a, parity);
-        } else {
-            if (sup) mf_fused_kernel<false, false, true, CHECK><<<grid, block, 0, st>>>(a, parity);
-            else mf_fused_kernel<false, false, false, CHECK><<<grid, block, 0, st>>>(a, parity);
-        }
-    }
-}
-
-// ---- two iterations per launch (pairs.cuh) ------------------------------------
-// parity 0 reads the state set (hp, pt, u, tmp) and writes (hpB, ptB, uB,
-// tmpB); parity 1 the other way round.  2 blocks of 512 threads per SM (64
-// registers, 103 KB of shared memory each).
-template <bool ALPHA_ARR, bool SUPERVISED, bool CHECK>
-__global__ void __launch_bounds__(kPN, 2) mf_pair_kernel(MfArgs a, int parity)
-{
-    extern __shared__ __align__(16) unsigned char pair_smem[];
-    __shared__ float red[32];
-    if (__ldcg(&a.ctrl->stopped)) return;
-    PairView v;
-    v.d0 = a.d0; v.d1 = a.d1; v.d2 = a.d2; v.zc = a.zc;
-    v.rcc = a.rcc; v.rs0 = a.rs0; v.rs1 = a.rs1; v.rs2 = a.rs2; v.ss0 = a.ss0; v.ss1 = a.ss1; v.ss2 = a.ss2;
-    v.sq0 = a.sq0; v.sq1 = a.sq1; v.sq2 = a.sq2; v.isq0 = a.isq0; v.isq1 = a.isq1; v.isq2 = a.isq2;
-    v.alpha_scalar = a.alpha_scalar;
-    v.q4 = a.q4; v.alpha = a.alpha; v.cs = a.cs; v.ct = a.ct; v.labels = a.labels;
-    float *A[6] = {a.hp0, a.hp1, a.hp2, a.pt, a.u, a.tmp};
-    float *B[6] = {a.hpB0, a.hpB1, a.hpB2, a.ptB, a.uB, a.tmpB};
-    float **in = parity ? B : A, **out = parity ? A : B;
-    v.hp0_in = in[0]; v.hp1_in = in[1]; v.hp2_in = in[2]; v.pt_in = in[3]; v.u_in = in[4]; v.tmp_in = in[5];
-    v.hp0_out = out[0]; v.hp1_out = out[1]; v.hp2_out = out[2]; v.pt_out = out[3]; v.u_out = out[4];
-    v.tmp_out = out[5];
-    const float acc = pair_tile<ALPHA_ARR, SUPERVISED, CHECK>(v, pair_smem);
-    if (CHECK) {
-        const float s = block_sum(acc, red);
-        if (threadIdx.x == 0 && threadIdx.y == 0)
-            a.partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
-    }
-}
-
-template <bool ALPHA_ARR, bool SUPERVISED, bool CHECK>
-cudaError_t launch_pair_t(dim3 grid, cudaStream_t st, const MfArgs &a, int parity)
-{
-    // the shared-memory opt-in is per device: done once for each
-    static std::atomic<uint64_t> opted{0};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
-    if (!bit || !(opted.load() & bit)) {
-        e = cudaFuncSetAttribute(mf_pair_kernel<ALPHA_ARR, SUPERVISED, CHECK>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPairSmem);
-        if (e != cudaSuccess) return e;
-        opted.fetch_or(bit);
-    }
-    mf_pair_kernel<ALPHA_ARR, SUPERVISED, CHECK><<<grid, dim3(kPX, kPY, 1), kPairSmem, st>>>(a, parity);
-    return cudaGetLastError();
-}
-
-inline cudaError_t launch_pair(bool alpha_arr, bool sup, bool check, dim3 grid, cudaStream_t st, const MfArgs &a,
-                               int parity)
-{
-    if (alpha_arr) {
-        if (sup) return check ? launch_pair_t<true, true, true>(grid, st, a, parity)
-                              : launch_pair_t<true, true, false>(grid, st, a, parity);
-        return check ? launch_pair_t<true, false, true>(grid, st, a, parity)
-                     : launch_pair_t<true, false, false>(grid, st, a, parity);
-    }
-    if (sup) return check ? launch_pair_t<false, true, true>(grid, st, a, parity)
-                          : launch_pair_t<false, true, false>(grid, st, a, parity);
-    return check ? launch_pair_t<false, false, true>(grid, st, a, parity)
-                 : launch_pair_t<false, false, false>(grid, st, a, parity);
-}
-
 // residual = sum(partials) / (N * rcc); stop on NaN or below the bound
 // (continuous_cut_anisotropic_gpu.py:321-337)
 __global__ void mf_check_kernel(const float *__restrict__ part, int nparts, double inv_norm, double bound,
@@ -339,14 +211,9 @@ __global__ void mf_check_kernel(const float *__restrict__ part, int nparts, doub
 // ---- host side --------------------------------------------------------------
 
 struct MfLayout {
-    size_t hp0, hp1, hp2, pt, tmp, hpB0, hpB1, hpB2, tmpB, ptB, uB, q4, partials, maxpart, ctrl, resid, total;
+    size_t hp0, hp1, hp2, pt, tmp, q4, partials, maxpart, ctrl, resid, total;
     int nparts, resid_cap;
 };
-
-// what the workspace must hold besides the two-sweep state
-enum MfSets { kSetsSweeps = 0, kSetsFused = 1, kSetsPairs = 2 };
-// the path of M16_PATH_DEFAULT
-constexpr int kDefaultSets = kSetsSweeps;
 
 constexpr int kMaxBlocks = 4 * kSMs;
 
@@ -362,45 +229,19 @@ inline int choose_zc(int d0, int d1, int d2)
     return (int)zc;
 }
 
-// z-planes per block of the pair kernel: about 4 waves of 2 blocks per SM,
-// 16 to 64 planes (the block recomputes 3 planes of the first iteration
-// below its chunk and 1 above, so longer chunks waste less)
-inline int choose_pair_zc(int d0, int d1, int d2)
-{
-    const int64_t tiles = div_up(d2, kPIX) * div_up(d1, kPIY);
-    int64_t zc = div_up((int64_t)d0 * tiles, 4 * 2 * kSMs);
-    zc = std::max<int64_t>(16, std::min<int64_t>(64, zc));
-    return (int)std::min<int64_t>(zc, d0);
-}
-
-inline int64_t pair_blocks(int d0, int d1, int d2, int zc)
-{
-    return div_up(d2, kPIX) * div_up(d1, kPIY) * div_up(d0, zc);
-}
-
-// sets: the second state set of the fused iteration (hp, tmp) or of the pair
-// kernel (hp, pt, u, tmp) besides the two-sweep state; the block partials
-// cover the largest grid of any path
-inline MfLayout mf_layout(int d0, int d1, int d2, int num_iter, int update, int sets)
+// the two-sweep state, the expanded quaternions, the block partials and the
+// residual log
+inline MfLayout mf_layout(int d0, int d1, int d2, int num_iter, int update)
 {
     MfLayout L;
     const int64_t n = (int64_t)d0 * d1 * d2;
     const int zc = choose_zc(d0, d1, d2);
     L.nparts = (int)(div_up(d2, kBX) * div_up(d1, kBY) * div_up(d0, zc));
-    if (sets == kSetsPairs) {
-        // every pair z-chunk length the caller may choose (at least 1 plane)
-        L.nparts = (int)std::max<int64_t>(L.nparts, pair_blocks(d0, d1, d2, 1));
-    }
     L.resid_cap = num_iter / (update > 0 ? update : 1) + 2;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
     L.hp0 = take(n * 4); L.hp1 = take(n * 4); L.hp2 = take(n * 4);
     L.pt = take(n * 4); L.tmp = take(n * 4);
-    L.hpB0 = L.hpB1 = L.hpB2 = L.tmpB = L.ptB = L.uB = 0;
-    if (sets != kSetsSweeps) {
-        L.hpB0 = take(n * 4); L.hpB1 = take(n * 4); L.hpB2 = take(n * 4); L.tmpB = take(n * 4);
-    }
-    if (sets == kSetsPairs) { L.ptB = take(n * 4); L.uB = take(n * 4); }
     L.q4 = take(n * 16);
     L.partials = take((size_t)L.nparts * 4);
     L.maxpart = take(kMaxBlocks * 4);
@@ -420,7 +261,7 @@ using namespace m16;
 extern "C" size_t m16_maxflow_workspace_bytes(int32_t d0, int32_t d1, int32_t d2, const m16_cut_params *params)
 {
     if (d0 < 1 || d1 < 1 || d2 < 1 || !params) return 0;
-    return mf_layout(d0, d1, d2, params->num_iter, params->update, kSetsPairs).total;
+    return mf_layout(d0, d1, d2, params->num_iter, params->update).total;
 }
 
 extern "C" int m16_maxflow_solve(const float *img, const float *quat3, const double *sqevals3,
@@ -454,16 +295,13 @@ struct EventPool {
 };
 }  // namespace
 
-// The solve.  path: kSetsSweeps (every iteration a flow and a label launch),
-// kSetsFused (one launch per iteration, fused.cuh) or kSetsPairs (two
-// iterations per launch, pairs.cuh, wherever no residual check falls on the
-// pair's first iteration; the other iterations as two sweeps).
+// The solve: every iteration a flow and a label launch.
 static int maxflow_solve_impl(const float *img, const float *quat3, const double *sqevals3, const float *sqeigs,
                               const float *alpha, float alpha_scalar, const float *cs, const float *ct,
                               const uint8_t *labels, int32_t d0, int32_t d1, int32_t d2,
                               const m16_cut_params *params, float *u, int32_t *iterations, double *residuals,
                               int32_t residuals_cap, int32_t *n_residuals, void *workspace, size_t workspace_bytes,
-                              void *stream, m16_solve_stats *stats, int path)
+                              void *stream, m16_solve_stats *stats)
 {
     if (d0 < 1 || d1 < 1 || d2 < 1) return M16_ERR_BAD_SHAPE;
     if ((int64_t)d0 * d1 * d2 > ((int64_t)1 << 34)) return M16_ERR_BAD_SHAPE;
@@ -476,11 +314,7 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
     if (sqevals3)
         for (int k = 0; k < 3; ++k)
             if (!finite_pos(sqevals3[k])) return M16_ERR_BAD_ARG;
-    if (path == kSetsPairs && sqevals3 == nullptr) path = kSetsSweeps;   // per-voxel eigenvalues: two sweeps
-    const bool fused = path == kSetsFused, pairs = path == kSetsPairs;
-    int pair_zc = choose_pair_zc(d0, d1, d2);
-    if (pairs && stats && stats->pair_zc > 0) pair_zc = std::min<int>(stats->pair_zc, d0);
-    const MfLayout L = mf_layout(d0, d1, d2, params->num_iter, params->update, path);
+    const MfLayout L = mf_layout(d0, d1, d2, params->num_iter, params->update);
     if (!workspace || workspace_bytes < L.total || ((uintptr_t)workspace & 255)) return M16_ERR_WORKSPACE;
     cudaStream_t st = (cudaStream_t)stream;
     char *ws = (char *)workspace;
@@ -503,13 +337,6 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
     a.alpha_scalar = alpha_scalar;
     a.hp0 = (float *)(ws + L.hp0); a.hp1 = (float *)(ws + L.hp1); a.hp2 = (float *)(ws + L.hp2);
     a.pt = (float *)(ws + L.pt); a.tmp = (float *)(ws + L.tmp); a.u = u;
-    const bool second_set = path != kSetsSweeps;
-    a.hpB0 = second_set ? (float *)(ws + L.hpB0) : nullptr;
-    a.hpB1 = second_set ? (float *)(ws + L.hpB1) : nullptr;
-    a.hpB2 = second_set ? (float *)(ws + L.hpB2) : nullptr;
-    a.tmpB = second_set ? (float *)(ws + L.tmpB) : nullptr;
-    a.ptB = pairs ? (float *)(ws + L.ptB) : nullptr;
-    a.uB = pairs ? (float *)(ws + L.uB) : nullptr;
     a.q4 = (const float4 *)(ws + L.q4);
     a.alpha = alpha; a.sqeigs = sqeigs; a.cs = cs; a.ct = ct; a.labels = labels;
     a.partials = (float *)(ws + L.partials);
@@ -522,18 +349,9 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
     mf_init_kernel<<<init_blocks, 256, 0, st>>>(a, img, quat3, n);
     M16_CUDA_TRY(cudaGetLastError());
 
-    // the two-sweep arguments over the second state set of the pair path
-    MfArgs b = a;
-    if (pairs) {
-        b.hp0 = a.hpB0; b.hp1 = a.hpB1; b.hp2 = a.hpB2; b.pt = a.ptB; b.u = a.uB; b.tmp = a.tmpB;
-    }
-    MfArgs pa = a;
-    pa.zc = pair_zc;
-
     const dim3 block(kBX, kBY, 1);
     const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)div_up(d0, a.zc));
-    const dim3 pgrid((unsigned)div_up(d2, kPIX), (unsigned)div_up(d1, kPIY), (unsigned)div_up(d0, pair_zc));
-    const int nparts_sweep = (int)(grid.x * grid.y * grid.z), nparts_pair = (int)(pgrid.x * pgrid.y * pgrid.z);
+    const int nparts_sweep = (int)(grid.x * grid.y * grid.z);
     const bool pointwise = sqevals3 == nullptr;
     const bool alpha_arr = alpha != nullptr;
     const bool sup = labels != nullptr;
@@ -548,64 +366,21 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
         pool.reset(new EventPool(3 * chunk));
         if (!pool->ok) return M16_ERR_CUDA;
     }
-    int launches = 3, p_launches = 0, u_launches = 0, pair_launches = 0;
-    double p_ms = 0.0, u_ms = 0.0, pair_ms = 0.0;
-    // the pair path's launches: (first iteration, two iterations?) in order;
-    // which state set ends the solve follows from the iterations that ran
-    std::vector<int> pair_starts;
-    int cur = 0;   // the state set the next launch reads: 0 = a (u is the caller's), 1 = b
+    int launches = 3, p_launches = 0, u_launches = 0;
+    double p_ms = 0.0, u_ms = 0.0;
 
     MfCtrl hctrl;
     hctrl.stopped = 0;
     int it = 0;
     while (it < params->num_iter) {
         const int end = std::min(params->num_iter, it + chunk);
-        // per launch slot: (start iteration, kind 0 sweeps / 1 pair), for the timing
-        std::vector<int> slot_it, slot_kind;
+        // per launch slot: its iteration, for the timing
+        std::vector<int> slot_it;
         while (it < end) {
             const int j = (int)slot_it.size();
             if (timing) cudaEventRecord(pool->ev[3 * j], st);
-            // a pair may end one iteration past the chunk: chunks only pace the host's polls
-            if (pairs && (it % update) != 0 && it + 1 < params->num_iter) {
-                const bool check = ((it + 1) % update) == 0;
-                M16_CUDA_TRY(launch_pair(alpha_arr, sup, check, pgrid, st, pa, cur));
-                if (timing) {
-                    cudaEventRecord(pool->ev[3 * j + 1], st);
-                    cudaEventRecord(pool->ev[3 * j + 2], st);
-                }
-                if (check) {
-                    mf_check_kernel<<<1, 256, 0, st>>>(a.partials, nparts_pair, inv_norm, params->error_bound, it + 1,
-                                                       (it + 1) / update, L.resid_cap, a.ctrl, resid);
-                    ++launches;
-                }
-                ++launches;
-                pair_starts.push_back(it);
-                slot_it.push_back(it);
-                slot_kind.push_back(1);
-                cur ^= 1;
-                it += 2;
-                continue;
-            }
             slot_it.push_back(it);
-            slot_kind.push_back(0);
-            if (fused) {
-                const bool check = (it % update) == 0;
-                if (check) launch_fused<true>(pointwise, alpha_arr, sup, grid, st, a, it & 1);
-                else launch_fused<false>(pointwise, alpha_arr, sup, grid, st, a, it & 1);
-                if (timing) {
-                    cudaEventRecord(pool->ev[3 * j + 1], st);
-                    cudaEventRecord(pool->ev[3 * j + 2], st);
-                }
-                if (check) {
-                    mf_check_kernel<<<1, 256, 0, st>>>(a.partials, L.nparts, inv_norm, params->error_bound, it,
-                                                       it / update, L.resid_cap, a.ctrl, resid);
-                    ++launches;
-                }
-                ++launches;
-                ++it;
-                continue;
-            }
-            const MfArgs &s = cur ? b : a;
+            const MfArgs &s = a;
             if (pointwise) {
                 if (alpha_arr) M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<true, true>, grid, block, st, pdl, s));
                 else M16_CUDA_TRY(launch_pdl(mf_update_p_kernel<true, false>, grid, block, st, pdl, s));
@@ -642,15 +417,10 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
                 float a_ms = 0.f, b_ms = 0.f;
                 M16_CUDA_TRY(cudaEventElapsedTime(&a_ms, pool->ev[3 * j], pool->ev[3 * j + 1]));
                 M16_CUDA_TRY(cudaEventElapsedTime(&b_ms, pool->ev[3 * j + 1], pool->ev[3 * j + 2]));
-                if (slot_kind[j]) {
-                    pair_ms += a_ms;
-                    ++pair_launches;
-                } else {
-                    p_ms += a_ms;
-                    u_ms += b_ms;
-                    ++p_launches;
-                    ++u_launches;
-                }
+                p_ms += a_ms;
+                u_ms += b_ms;
+                ++p_launches;
+                ++u_launches;
             }
         }
         if (hctrl.stopped) break;
@@ -658,29 +428,16 @@ static int maxflow_solve_impl(const float *img, const float *quat3, const double
     M16_CUDA_TRY(cudaMemcpyAsync(&hctrl, a.ctrl, sizeof(MfCtrl), cudaMemcpyDeviceToHost, st));
     M16_CUDA_TRY(cudaStreamSynchronize(st));
     const int ran = hctrl.stopped ? hctrl.iterations : it;
-    // the pair launches that ran each switched the state set
-    int pairs_ran = 0;
-    for (int s0 : pair_starts)
-        if (s0 < ran) ++pairs_ran;
-    if (pairs_ran & 1) {
-        M16_CUDA_TRY(cudaMemcpyAsync(u, a.uB, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
-        M16_CUDA_TRY(cudaStreamSynchronize(st));
-        ++launches;
-    }
     if (stats) {
         stats->launches = launches;
-        if (!timing) {
-            pair_launches = pairs_ran;
-            p_launches = std::max(0, ran - 2 * pairs_ran);
-            u_launches = fused ? 0 : p_launches;
-        }
+        if (!timing) p_launches = u_launches = ran;
         stats->p_launches = p_launches;
-        stats->u_launches = fused ? 0 : u_launches;
+        stats->u_launches = u_launches;
         stats->p_ms = p_ms;
         stats->u_ms = u_ms;
-        stats->pair_launches = pair_launches;
-        stats->pair_ms = pair_ms;
-        stats->pair_zc = pairs ? pair_zc : 0;
+        stats->pair_launches = 0;
+        stats->pair_ms = 0.0;
+        stats->pair_zc = 0;
     }
     *iterations = hctrl.iterations;
     if (n_residuals) *n_residuals = hctrl.n_checks;
@@ -702,15 +459,12 @@ extern "C" int m16_maxflow_solve_ex(const float *img, const float *quat3, const 
                                     int32_t *n_residuals, void *workspace, size_t workspace_bytes, void *stream,
                                     m16_solve_stats *stats)
 {
-    if (stats && (stats->path < M16_PATH_DEFAULT || stats->path > M16_PATH_PAIRS)) return M16_ERR_BAD_ARG;
-    const int want = stats ? stats->path : M16_PATH_DEFAULT;
-    const int path = want == M16_PATH_FUSED ? kSetsFused
-                     : want == M16_PATH_TWO_SWEEPS ? kSetsSweeps
-                     : want == M16_PATH_PAIRS ? kSetsPairs
-                                              : kDefaultSets;
+    // the two sweeps are the only iteration path (the fused iteration and two
+    // iterations per launch measured slower at every size and were removed)
+    if (stats && stats->path != M16_PATH_DEFAULT && stats->path != M16_PATH_TWO_SWEEPS) return M16_ERR_BAD_ARG;
     return maxflow_solve_impl(img, quat3, sqevals3, sqeigs, alpha, alpha_scalar, cs, ct, labels, d0, d1, d2, params,
                               u, iterations, residuals, residuals_cap, n_residuals, workspace, workspace_bytes,
-                              stream, stats, path);
+                              stream, stats);
 }
 
 // ---- fixed-footprint variant: no allocation by anyone --------------------------
@@ -771,7 +525,7 @@ extern "C" int m16_maxflow_solve_static(const float *img, const float *quat3, co
     if (params->update < 1 || params->num_iter < 0) return M16_ERR_BAD_ARG;
     if ((int64_t)d0 * d1 * d2 > kStaticMaxVoxels) return M16_ERR_TOO_LARGE;
     if (params->num_iter / params->update + 2 > kStaticMaxChecks) return M16_ERR_TOO_LARGE;
-    const MfLayout L = mf_layout(d0, d1, d2, params->num_iter, params->update, kSetsSweeps);
+    const MfLayout L = mf_layout(d0, d1, d2, params->num_iter, params->update);
     if (L.total > kStaticBytes) return M16_ERR_TOO_LARGE;
     void *scratch = nullptr;
     const int st = static_scratch_on_current_device(&scratch);
@@ -782,5 +536,5 @@ extern "C" int m16_maxflow_solve_static(const float *img, const float *quat3, co
     // the two-sweep iteration: its workspace fits the fixed array
     return maxflow_solve_impl(img, quat3, sqevals3, sqeigs, alpha, alpha_scalar, cs, ct, labels, d0, d1, d2, params,
                               u, iterations, residuals, residuals_cap, n_residuals, scratch, kStaticBytes, stream,
-                              nullptr, kSetsSweeps);
+                              nullptr);
 }
