@@ -26,13 +26,15 @@ namespace {
 
 constexpr int kBX = 32, kBY = 8;
 
-// float(sin(xd)) and float(cos(xd)) of the double xd = x: single precision
-// where certain, double precision otherwise
-__device__ __forceinline__ void sincos_ref(float x, double xd, float *s, float *c)
+// float(sin(x)) and float(cos(x)) of x = (double)v * scale (scale 1 or 0.5):
+// single precision where certain, double precision otherwise.  The double
+// argument is formed only on the fallback path, so the common path issues no
+// FP64 instruction (FP64 runs at a small fraction of the FP32 rate).
+__device__ __forceinline__ void sincos_ref(float v, float scale, float *s, float *c)
 {
-    if (ff::sincos_rn(x, s, c)) return;
+    if (ff::sincos_rn(__fmul_rn(v, scale), s, c)) return;
     double sd, cd;
-    sincos(xd, &sd, &cd);
+    sincos((double)v * (double)scale, &sd, &cd);
     *s = (float)sd;
     *c = (float)cd;
 }
@@ -46,9 +48,9 @@ __device__ __forceinline__ void qexpand_ref(float phi, float theta, float psi, f
     const float pp = __fmul_rn(__fadd_rn(phi, psi), 0.5f);
     const float pm = __fmul_rn(__fsub_rn(phi, psi), 0.5f);
     float ct, st, cpp, spp, cpm, spm;
-    sincos_ref(__fmul_rn(theta, 0.5f), (double)theta * 0.5, &st, &ct);
-    sincos_ref(pp, (double)pp, &spp, &cpp);
-    sincos_ref(pm, (double)pm, &spm, &cpm);
+    sincos_ref(theta, 0.5f, &st, &ct);
+    sincos_ref(pp, 1.0f, &spp, &cpp);
+    sincos_ref(pm, 1.0f, &spm, &cpm);
     q[0] = __fmul_rn(cpp, ct);
     q[1] = __fmul_rn(cpm, st);
     q[2] = __fmul_rn(spm, st);
@@ -86,7 +88,7 @@ __device__ __forceinline__ void quat_cols(const float q[4], float c0[3], float c
 __global__ void __launch_bounds__(kBX * kBY) dr_detect_ridges_kernel(const float *__restrict__ resp,
                                                                      const float *__restrict__ quat3,
                                                                      float *__restrict__ ridge, int d0, int d1,
-                                                                     int d2, double threshold,
+                                                                     int d2, float threshold,
                                                                      float *__restrict__ dirs3)
 {
     const int x = blockIdx.x * kBX + threadIdx.x;
@@ -132,7 +134,9 @@ __global__ void __launch_bounds__(kBX * kBY) dr_detect_ridges_kernel(const float
         maxv = v > maxv ? v : maxv;
     }
     const float r = resp[i];
-    ridge[i] = ((double)r > threshold && r > maxv) ? 1.f : 0.f;
+    // threshold: the largest float not above the reference's double
+    // threshold, so r > threshold exactly when (double)r exceeds it
+    ridge[i] = (r > threshold && r > maxv) ? 1.f : 0.f;
 }
 
 // ---- extractMainDirections ----------------------------------------------------
@@ -535,6 +539,18 @@ inline int blocks1d(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64
 
 using namespace m16;
 
+namespace {
+// the largest float not above t (NaN for NaN): for every float r,
+// r > float_at_or_below(t) exactly when (double)r > t
+float float_at_or_below(double t)
+{
+    if (t != t) return NAN;
+    float f = (float)t;
+    if ((double)f > t) f = nextafterf(f, -INFINITY);
+    return f;
+}
+}  // namespace
+
 extern "C" int m16_detect_ridges(const float *resp, const float *quat3, int32_t d0, int32_t d1, int32_t d2,
                                  double threshold, float *ridge, void *stream)
 {
@@ -542,7 +558,8 @@ extern "C" int m16_detect_ridges(const float *resp, const float *quat3, int32_t 
     if (!resp || !quat3 || !ridge) return M16_ERR_BAD_ARG;
     const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)d0);
     dr_detect_ridges_kernel<<<grid, dim3(kBX, kBY, 1), 0, (cudaStream_t)stream>>>(resp, quat3, ridge, d0, d1, d2,
-                                                                                 threshold, nullptr);
+                                                                                 float_at_or_below(threshold),
+                                                                                 nullptr);
     M16_CUDA_TRY(cudaGetLastError());
     return M16_OK;
 }
@@ -554,7 +571,8 @@ extern "C" int m16_detect_ridges_main_directions(const float *resp, const float 
     if (!resp || !quat3 || !ridge || !dirs3) return M16_ERR_BAD_ARG;
     const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)d0);
     dr_detect_ridges_kernel<<<grid, dim3(kBX, kBY, 1), 0, (cudaStream_t)stream>>>(resp, quat3, ridge, d0, d1, d2,
-                                                                                 threshold, dirs3);
+                                                                                 float_at_or_below(threshold),
+                                                                                 dirs3);
     M16_CUDA_TRY(cudaGetLastError());
     return M16_OK;
 }

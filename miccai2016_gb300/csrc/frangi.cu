@@ -247,6 +247,11 @@ struct FrArgs {
 };
 
 // ---- pass 3: x (axis 2) fused with the eigensolve ----------------------------
+// One lane per voxel.  The Jacobi's data-dependent sweep count makes a warp
+// wait for its slowest voxel (21 of 32 lanes active on average).  Handing
+// each lane the next matrix of a per-warp pool as its own converges raised
+// that to 25 of 32 but added as many instructions as it saved (895 M -> 910
+// M warp instructions at 256^3, sigma 1, still issue-bound): no faster.
 template <bool FUSED_UPDATE>
 __global__ void __launch_bounds__(kBX * kBY) fr_conv_x_eig_kernel(FrArgs a, AxisTaps tp)
 {
