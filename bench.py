@@ -908,8 +908,8 @@ def run_paths(args, cfg):
     sq = (ctypes.c_double * 3)(*np.sqrt(P.ATV_EIGS).tolist())
     stream = torch.cuda.current_stream()
 
-    def solve(timing=0, flags=0):
-        s = N.SolveStats(timing, 0, 0, 0, 0.0, 0.0, N.PATH_DEFAULT, flags)
+    def solve(timing=0, flags=0, path=N.PATH_TWO_SWEEPS):
+        s = N.SolveStats(timing, 0, 0, 0, 0.0, 0.0, path, flags)
         it = ctypes.c_int32(0)
         st = L.m16_maxflow_solve_ex(N.ptr(d["img"]), N.ptr(d["quats"]), sq, None, N.ptr(d["alpha"]), 0.0,
                                     N.ptr(d["cs"]), N.ptr(d["ct"]), None, shape[0], shape[1], shape[2],
@@ -918,17 +918,17 @@ def run_paths(args, cfg):
         N.check("m16_maxflow_solve_ex", st)
         return s
 
-    def timed(flags=0):
+    def timed(flags=0, path=N.PATH_TWO_SWEEPS):
         for _ in range(args.warmup):
-            solve(flags=flags)
+            solve(flags=flags, path=path)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            s = solve(flags=flags)
+            s = solve(flags=flags, path=path)
         e1.record(stream)
         torch.cuda.synchronize()
-        k = solve(timing=1, flags=flags)
+        k = solve(timing=1, flags=flags, path=path)
         return dict(ms_per_solve=e0.elapsed_time(e1) / args.steps, launches=s.launches,
                     flow_sweep_ms=k.p_ms / max(k.p_launches, 1), label_sweep_ms=k.u_ms / max(k.u_launches, 1))
 
