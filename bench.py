@@ -508,8 +508,13 @@ def run_batched_grid():
     best_dice_true = dice_largest(us[best], truth_d)
     dice_largest_s = time.perf_counter() - t_dl
     del us
+    # the autotuner's candidates, each as a fixed tile shape for the whole
+    # solve, and the tuned shape without graph replay
     variants = {}
-    for name, kw in (("default_tile_shape", dict(tune=False)), ("no_graphs", dict(graphs=False))):
+    for name, kw in (("tile_8_blocks_per_sm", dict(tune=False, blocks_per_sm=8)),
+                     ("tile_16_blocks_per_sm", dict(tune=False, blocks_per_sm=16)),
+                     ("tile_32_blocks_per_sm", dict(tune=False, blocks_per_sm=32)),
+                     ("no_graphs", dict(graphs=False))):
         vu, vit, vs = _timed_batch(bc, [vol], insts, **kw)
         variants[name] = {"s": vs, "blocks_per_sm": bc.last_blocks_per_sm,
                           "same_iterations": bool(np.array_equal(vit, iters))}

@@ -110,7 +110,8 @@ typedef struct m16_solve_stats {
     int32_t path;          /* in: M16_PATH_* -- how an iteration is launched */
     int32_t flags;         /* in: M16_BATCH_* options of m16_batch_solve (0 elsewhere) */
     int32_t blocks_per_sm; /* out (m16_batch_solve): the sweeps' tile shape in use at the end, as the
-                              target blocks per SM its z-chunk was chosen for */
+                              target blocks per SM its z-chunk was chosen for; in, with
+                              M16_BATCH_NO_TUNE: 8, 16 or 32 fixes that shape (0: the default) */
     int32_t pair_launches; /* reserved (0): kept for the layout of ABI versions 3 and 4 */
     double pair_ms;        /* reserved (0) */
     int32_t pair_zc;       /* reserved (0) */

@@ -41,7 +41,7 @@ class BatchedCut(object):
                     grad2=None if grad2 is None else N.to_device_f32(grad2, shape),
                     scaling=(1.0, 1.0, 1.0) if scaling is None else tuple(float(v) for v in scaling))
 
-    def solve(self, volumes, instances, time_kernels=False, path=None, graphs=True, tune=True):
+    def solve(self, volumes, instances, time_kernels=False, path=None, graphs=True, tune=True, blocks_per_sm=0):
         """volumes: list of prepare_volume() dicts; instances: list of dicts
         with 'volume' (index), 'eigs' (3 constant eigenvalues) and either
         ('weighting', 'decay') or 'alpha' (an array of the volume's shape).
@@ -50,8 +50,9 @@ class BatchedCut(object):
         four interleaved instances).  graphs=False launches every iteration
         directly instead of replaying CUDA graphs of whole check intervals;
         tune=False keeps the default tile shape instead of timing the
-        candidates on the first check intervals (last_blocks_per_sm reports
-        the shape in use).
+        candidates on the first check intervals, or the shape of
+        blocks_per_sm (8, 16 or 32: one of the tuner's candidates);
+        last_blocks_per_sm reports the shape in use.
         Returns the list of u (CUDA tensors) in instance order."""
         torch = N.torch_mod()
         L = N.lib()
@@ -89,6 +90,8 @@ class BatchedCut(object):
         stats = N.SolveStats(int(bool(time_kernels)), 0, 0, 0, 0.0, 0.0,
                              N.PATH_DEFAULT if path is None else int(path),
                              (0 if graphs else N.BATCH_NO_GRAPH) | (0 if tune else N.BATCH_NO_TUNE))
+        if not tune:
+            stats.blocks_per_sm = int(blocks_per_sm)
         st = L.m16_batch_solve(vd, nv, idesc, ni, ctypes.byref(cp), iters, res, N.ptr(self._ws), self._ws.numel(),
                                N.stream_ptr(), ctypes.byref(stats))
         N.check("m16_batch_solve", st)

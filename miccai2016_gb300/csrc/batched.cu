@@ -484,6 +484,14 @@ extern "C" int m16_batch_solve(const m16_batch_volume *vols, int32_t nvol, const
     tune_key.push_back(params->update);
     int start_bps = M16_BATCH_BLOCKS_PER_SM;
     bool tune = false;
+    if (stats && (stats->flags & M16_BATCH_NO_TUNE) && stats->blocks_per_sm > 0) {
+        // a fixed tile shape: one of the tuner's candidates (the workspace is
+        // sized for them)
+        bool known = false;
+        for (int c : kTuneBps) known = known || c == stats->blocks_per_sm;
+        if (!known) return M16_ERR_BAD_ARG;
+        start_bps = stats->blocks_per_sm;
+    }
     if (!(stats && (stats->flags & M16_BATCH_NO_TUNE))) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto f = g_tuned.find(tune_key);

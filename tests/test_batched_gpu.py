@@ -277,3 +277,30 @@ def test_batch_stopping_matches_the_oracle():
             same += 1
             assert np.max(np.abs(us[k] - u)) <= U_TOL, k
     assert same >= len(insts) - 1
+
+
+def test_fixed_tile_shapes_give_the_same_bits():
+    """Each of the autotuner's candidate tile shapes, fixed for the whole
+    solve, gives the same u (the tile only changes which block computes a
+    voxel; only the residual's partial sums follow the tiling); a shape
+    outside the candidates is rejected."""
+    import ctypes
+    from miccai2016_gb300 import _native as N
+    from miccai2016_gb300.batched import BatchedCut
+    vols = [_volume(31, (40, 36, 44))]
+    insts = [dict(volume=0, weighting=w, decay=d, eigs=ATV) for w in (0.02, 0.2) for d in (1.0, 30.0, 300.0)]
+    p = BatchedCut.CutParameters()
+    p.num_iter, p.update, p.error_bound = 150, 30, -1.0   # fixed iterations: the residual sums' tiling differs
+    b = BatchedCut(p)
+    dv = [b.prepare_volume(v["img"], v["quats"], v["cs"], v["ct"], grad2=v["grad2"]) for v in vols]
+    out = {}
+    for bps in (8, 16, 32):
+        us = b.solve(dv, insts, tune=False, blocks_per_sm=bps)
+        assert b.last_blocks_per_sm == bps
+        out[bps] = ([u.cpu().numpy() for u in us], b.last_iterations.copy())
+    for bps in (8, 32):
+        assert np.array_equal(out[bps][1], out[16][1])
+        for k in range(len(insts)):
+            assert np.array_equal(out[bps][0][k], out[16][0][k]), (bps, k)
+    with pytest.raises(N.M16Error):
+        b.solve(dv, insts, tune=False, blocks_per_sm=12)
