@@ -15,4 +15,4 @@ extern "C" const char *m16_status_string(int status)
     }
 }
 
-extern "C" int m16_abi_version(void) { return 4; }
+extern "C" int m16_abi_version(void) { return 5; }
