@@ -246,12 +246,56 @@ struct FrArgs {
     const float *c_dev;
 };
 
+// eigensolve of one Hessian and its output: the running maximum update
+// when c is given, else the eigen-triple stored for the update after c is
+// known, its norm folded into mx (calculateNorm, frangi.cl)
+template <bool FUSED_UPDATE>
+__device__ __forceinline__ void x_epilogue(const FrArgs &a, const float h[6], int64_t i, float &mx)
+{
+    float e[6];
+    eig3(h, e);
+    if (FUSED_UPDATE) {
+        const float v = vesselness(e, a.alpha, a.beta, a.c, a.bright != 0);
+        if (v > a.val[i]) {
+            a.val[i] = v;
+            a.quat3[3 * i] = e[3];
+            a.quat3[3 * i + 1] = e[4];
+            a.quat3[3 * i + 2] = e[5];
+        }
+    } else {
+        float2 *o = reinterpret_cast<float2 *>(a.eig6 + 6 * i);
+        o[0] = make_float2(e[0], e[1]);
+        o[1] = make_float2(e[2], e[3]);
+        o[2] = make_float2(e[4], e[5]);
+        // calculateNorm + redMax (NaN-neutral)
+        mx = fmaxf(mx, sqrtf(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]));
+    }
+}
+
+// block maximum of the norms into the block's partial (redMax, max.cl);
+// fmaxf ignores NaN as the reference's fmax does
+__device__ __forceinline__ void block_max_to_partial(float mx, float *red, float *partials)
+{
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0) red[tid >> 5] = mx;
+    __syncthreads();
+    if (tid == 0) {
+        float m = red[0];
+        for (int w = 1; w < (kBX * kBY) / 32; ++w) m = fmaxf(m, red[w]);
+        partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = m;
+    }
+}
+
 // ---- pass 3: x (axis 2) fused with the eigensolve ----------------------------
 // One lane per voxel.  The Jacobi's data-dependent sweep count makes a warp
 // wait for its slowest voxel (21 of 32 lanes active on average).  Handing
 // each lane the next matrix of a per-warp pool as its own converges raised
 // that to 25 of 32 but added as many instructions as it saved (895 M -> 910
 // M warp instructions at 256^3, sigma 1, still issue-bound): no faster.
+// This is the kernel for any radius; radii up to kRunMaxR take the
+// specialised fr_conv_x_eig_run_kernel below.
 template <bool FUSED_UPDATE>
 __global__ void __launch_bounds__(kBX * kBY) fr_conv_x_eig_kernel(FrArgs a, AxisTaps tp)
 {
@@ -279,40 +323,201 @@ __global__ void __launch_bounds__(kBX * kBY) fr_conv_x_eig_kernel(FrArgs a, Axis
                 h[4] = fmaf(t1, __ldg(a.six + 4 * n + idx), h[4]);
                 h[5] = fmaf(t1, __ldg(a.six + 5 * n + idx), h[5]);
             }
-            float e[6];
-            eig3(h, e);
-            const int64_t i = row + x;
-            if (FUSED_UPDATE) {
-                const float v = vesselness(e, a.alpha, a.beta, a.c, a.bright != 0);
-                if (v > a.val[i]) {
-                    a.val[i] = v;
-                    a.quat3[3 * i] = e[3];
-                    a.quat3[3 * i + 1] = e[4];
-                    a.quat3[3 * i + 2] = e[5];
-                }
-            } else {
-                float2 *o = reinterpret_cast<float2 *>(a.eig6 + 6 * i);
-                o[0] = make_float2(e[0], e[1]);
-                o[1] = make_float2(e[2], e[3]);
-                o[2] = make_float2(e[4], e[5]);
-                // calculateNorm + redMax (NaN-neutral)
-                mx = fmaxf(mx, sqrtf(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]));
+            x_epilogue<FUSED_UPDATE>(a, h, row + x, mx);
+        }
+    }
+    if (!FUSED_UPDATE) block_max_to_partial(mx, red, a.partials);
+}
+
+// ---- radius-specialised passes ------------------------------------------------
+// For radii 1..kRunMaxR every pass is instantiated per radius: the tap loops
+// unroll and the taps become constant operands.  The z and y passes keep a
+// run of outputs per thread and read each input once for the whole run
+// (kRun + 2R loads instead of kRun * (2R + 1)); the x pass stages each row
+// of the six products, with its halo, in the warp's own shared memory and
+// convolves from there.  Every output still accumulates its taps in the
+// same order (j = 0..K-1, tap K-1-j) with the same fused multiply-adds, so
+// the results equal the kernels above bit for bit.
+constexpr int kRunMaxR = 16;
+constexpr int kRun = 8;   // outputs per thread along z (z pass) or y (y pass)
+static_assert(2 * kRunMaxR <= kBX, "the x pass stages each row in two 32-column steps");
+
+template <int R, bool INNER>
+__device__ __forceinline__ void z_run(const float *__restrict__ col, int64_t s0, int za, int d0, const AxisTaps &tp,
+                                      float (&acc)[kRun][3])
+{
+    constexpr int K = 2 * R + 1;
+#pragma unroll
+    for (int p = 0; p < kRun + 2 * R; ++p) {
+        const int m = INNER ? za - R + p : mirror(za - R + p, d0);
+        const float v = __ldg(col + (int64_t)m * s0);
+#pragma unroll
+        for (int o = 0; o < kRun; ++o) {
+            const int j = p - o;
+            if (j >= 0 && j < K) {
+                acc[o][0] = fmaf(tp.t[0][K - 1 - j], v, acc[o][0]);
+                acc[o][1] = fmaf(tp.t[1][K - 1 - j], v, acc[o][1]);
+                acc[o][2] = fmaf(tp.t[2][K - 1 - j], v, acc[o][2]);
             }
         }
     }
-    if (!FUSED_UPDATE) {
-        // block maximum (fmaxf ignores NaN as the reference's fmax does)
-        const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+}
+
+template <int R>
+__global__ void __launch_bounds__(kBX * kBY) fr_conv_z_run_kernel(const float *__restrict__ img, float *__restrict__ z0,
+                                                                  float *__restrict__ z1, float *__restrict__ z2,
+                                                                  int d0, int d1, int d2, AxisTaps tp)
+{
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y * kBY + threadIdx.y;
+    if (x >= d2 || y >= d1) return;
+    const int za = blockIdx.z * kRun;
+    const int64_t s0 = (int64_t)d1 * d2;
+    const int64_t col = (int64_t)y * d2 + x;
+    float acc[kRun][3];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
-        if ((tid & 31) == 0) red[tid >> 5] = mx;
-        __syncthreads();
-        if (tid == 0) {
-            float m = red[0];
-            for (int w = 1; w < (kBX * kBY) / 32; ++w) m = fmaxf(m, red[w]);
-            a.partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = m;
+    for (int o = 0; o < kRun; ++o) acc[o][0] = acc[o][1] = acc[o][2] = 0.f;
+    if (za - R >= 0 && za + kRun - 1 + R < d0)
+        z_run<R, true>(img + col, s0, za, d0, tp, acc);
+    else
+        z_run<R, false>(img + col, s0, za, d0, tp, acc);
+#pragma unroll
+    for (int o = 0; o < kRun; ++o) {
+        if (za + o < d0) {
+            const int64_t i = col + (int64_t)(za + o) * s0;
+            z0[i] = acc[o][0];
+            z1[i] = acc[o][1];
+            z2[i] = acc[o][2];
         }
     }
+}
+
+template <int R, bool INNER>
+__device__ __forceinline__ void y_run(const float *__restrict__ z0, const float *__restrict__ z1,
+                                      const float *__restrict__ z2, int64_t plane, int d2, int ya, int d1,
+                                      const AxisTaps &tp, float (&acc)[kRun][6])
+{
+    constexpr int K = 2 * R + 1;
+#pragma unroll
+    for (int p = 0; p < kRun + 2 * R; ++p) {
+        const int m = INNER ? ya - R + p : mirror(ya - R + p, d1);
+        const int64_t idx = plane + (int64_t)m * d2;
+        const float v0 = __ldg(z0 + idx), v1 = __ldg(z1 + idx), v2 = __ldg(z2 + idx);
+#pragma unroll
+        for (int o = 0; o < kRun; ++o) {
+            const int j = p - o;
+            if (j >= 0 && j < K) {
+                const int k = K - 1 - j;
+                acc[o][0] = fmaf(tp.t[0][k], v2, acc[o][0]);   // A = y0 Z2
+                acc[o][1] = fmaf(tp.t[2][k], v0, acc[o][1]);   // B = y2 Z0
+                acc[o][2] = fmaf(tp.t[0][k], v0, acc[o][2]);   // C = y0 Z0
+                acc[o][3] = fmaf(tp.t[1][k], v1, acc[o][3]);   // D = y1 Z1
+                acc[o][4] = fmaf(tp.t[0][k], v1, acc[o][4]);   // E = y0 Z1
+                acc[o][5] = fmaf(tp.t[1][k], v0, acc[o][5]);   // F = y1 Z0
+            }
+        }
+    }
+}
+
+// grid (x blocks, y blocks of kBY runs of kRun rows, one z plane per block)
+template <int R>
+__global__ void __launch_bounds__(kBX * kBY) fr_conv_y_run_kernel(const float *__restrict__ z0,
+                                                                  const float *__restrict__ z1,
+                                                                  const float *__restrict__ z2,
+                                                                  float *__restrict__ six, int d0, int d1, int d2,
+                                                                  AxisTaps tp)
+{
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int ya = (blockIdx.y * kBY + threadIdx.y) * kRun;
+    if (x >= d2 || ya >= d1) return;
+    const int64_t s0 = (int64_t)d1 * d2, n = s0 * d0;
+    const int64_t plane = (int64_t)blockIdx.z * s0 + x;
+    float acc[kRun][6];
+#pragma unroll
+    for (int o = 0; o < kRun; ++o)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[o][c] = 0.f;
+    if (ya - R >= 0 && ya + kRun - 1 + R < d1)
+        y_run<R, true>(z0, z1, z2, plane, d2, ya, d1, tp, acc);
+    else
+        y_run<R, false>(z0, z1, z2, plane, d2, ya, d1, tp, acc);
+#pragma unroll
+    for (int o = 0; o < kRun; ++o) {
+        if (ya + o < d1) {
+            const int64_t i = plane + (int64_t)(ya + o) * d2;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) six[c * n + i] = acc[o][c];
+        }
+    }
+}
+
+// x pass fused with the eigensolve; warp w of the block works on row
+// y = blockIdx.y * kBY + w and stages its 32 + 2R columns of the six
+// products in shared memory (only __syncwarp between staging and reads)
+template <bool FUSED_UPDATE, int R>
+__global__ void __launch_bounds__(kBX * kBY) fr_conv_x_eig_run_kernel(FrArgs a, AxisTaps tp)
+{
+    constexpr int K = 2 * R + 1, W = kBX + 2 * R;
+    __shared__ float red[32];
+    __shared__ float rows[kBY][6][W];
+    const int lane = threadIdx.x;
+    const int x0 = blockIdx.x * kBX, x = x0 + lane;
+    const int y = blockIdx.y * kBY + threadIdx.y;
+    float mx = -INFINITY;
+    if (y < a.d1) {   // uniform over the warp
+        float (*buf)[W] = rows[threadIdx.y];
+        const int za = blockIdx.z * a.zc, zb = min(za + a.zc, a.d0);
+        const int64_t s0 = (int64_t)a.d1 * a.d2, n = s0 * a.d0;
+        const bool inner = x0 - R >= 0 && x0 + kBX - 1 + R < a.d2;
+        for (int z = za; z < zb; ++z) {
+            const int64_t row = (int64_t)z * s0 + (int64_t)y * a.d2;
+#pragma unroll
+            for (int i0 = 0; i0 < W; i0 += kBX) {
+                const int i = i0 + lane;
+                if (i < W) {
+                    const int m = inner ? x0 - R + i : mirror(x0 - R + i, a.d2);
+                    const float *src = a.six + row + m;
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) buf[c][i] = __ldg(src + c * n);
+                }
+            }
+            __syncwarp();
+            float h[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                const int k = K - 1 - j;
+                h[0] = fmaf(tp.t[0][k], buf[0][lane + j], h[0]);
+                h[1] = fmaf(tp.t[0][k], buf[1][lane + j], h[1]);
+                h[2] = fmaf(tp.t[2][k], buf[2][lane + j], h[2]);
+                h[3] = fmaf(tp.t[0][k], buf[3][lane + j], h[3]);
+                h[4] = fmaf(tp.t[1][k], buf[4][lane + j], h[4]);
+                h[5] = fmaf(tp.t[1][k], buf[5][lane + j], h[5]);
+            }
+            __syncwarp();
+            if (x < a.d2) x_epilogue<FUSED_UPDATE>(a, h, row + x, mx);
+        }
+    }
+    if (!FUSED_UPDATE) block_max_to_partial(mx, red, a.partials);
+}
+
+#define FR_RADIUS_CASES(CALL)                                                                                   \
+    case 1: CALL(1); break;   case 2: CALL(2); break;   case 3: CALL(3); break;   case 4: CALL(4); break;     \
+    case 5: CALL(5); break;   case 6: CALL(6); break;   case 7: CALL(7); break;   case 8: CALL(8); break;     \
+    case 9: CALL(9); break;   case 10: CALL(10); break; case 11: CALL(11); break; case 12: CALL(12); break;   \
+    case 13: CALL(13); break; case 14: CALL(14); break; case 15: CALL(15); break; case 16: CALL(16); break;
+
+// the x pass for one scale: the specialised kernel for radii 1..kRunMaxR,
+// else the kernel for any radius (same grid)
+template <bool FUSED_UPDATE>
+void launch_x_eig(const FrArgs &a, const AxisTaps &tpx, dim3 grid, cudaStream_t st)
+{
+    const dim3 block(kBX, kBY, 1);
+#define FR_X_CALL(R) fr_conv_x_eig_run_kernel<FUSED_UPDATE, R><<<grid, block, 0, st>>>(a, tpx)
+    switch (tpx.radius) {
+        FR_RADIUS_CASES(FR_X_CALL)
+        default: fr_conv_x_eig_kernel<FUSED_UPDATE><<<grid, block, 0, st>>>(a, tpx); break;
+    }
+#undef FR_X_CALL
 }
 
 // c = 0.5 * max norm of one scale (qfrangi_gpu.py:429-433)
@@ -438,8 +643,23 @@ int hessian_passes(const float *img, int d0, int d1, int d2, const float *taps, 
     const dim3 block(kBX, kBY, 1);
     const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)div_up(d0, zc));
     float *z = (float *)(ws + L.z);
-    fr_conv_z_kernel<<<grid, block, 0, st>>>(img, z, z + n, z + 2 * n, d0, d1, d2, zc, tpz);
-    fr_conv_y_kernel<<<grid, block, 0, st>>>(z, z + n, z + 2 * n, (float *)(ws + L.six), d0, d1, d2, zc, tpy);
+    float *six = (float *)(ws + L.six);
+    const dim3 grid_z((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)div_up(d0, kRun));
+#define FR_Z_CALL(R) fr_conv_z_run_kernel<R><<<grid_z, block, 0, st>>>(img, z, z + n, z + 2 * n, d0, d1, d2, tpz)
+    switch (tpz.radius) {
+        FR_RADIUS_CASES(FR_Z_CALL)
+        default: fr_conv_z_kernel<<<grid, block, 0, st>>>(img, z, z + n, z + 2 * n, d0, d1, d2, zc, tpz); break;
+    }
+#undef FR_Z_CALL
+    // one z plane per block of the specialised y pass (grid z limit 65535)
+    const dim3 grid_y((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY * kRun), (unsigned)d0);
+    const int ry = d0 <= 65535 ? tpy.radius : 0;
+#define FR_Y_CALL(R) fr_conv_y_run_kernel<R><<<grid_y, block, 0, st>>>(z, z + n, z + 2 * n, six, d0, d1, d2, tpy)
+    switch (ry) {
+        FR_RADIUS_CASES(FR_Y_CALL)
+        default: fr_conv_y_kernel<<<grid, block, 0, st>>>(z, z + n, z + 2 * n, six, d0, d1, d2, zc, tpy); break;
+    }
+#undef FR_Y_CALL
     M16_CUDA_TRY(cudaGetLastError());
     return M16_OK;
 }
@@ -476,17 +696,16 @@ extern "C" int m16_frangi(const float *img, int32_t d0, int32_t d1, int32_t d2, 
     a.val = val; a.quat3 = quat3;
     a.partials = (float *)(ws + L.part);
     float *cdev = (float *)(ws + L.cdev);
-    const dim3 block(kBX, kBY, 1);
     const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)div_up(d0, a.zc));
     for (int s = 0; s < nscales; ++s) {
         AxisTaps tpx;
         const int rc = hessian_passes(img, d0, d1, d2, taps + (size_t)s * 9 * kMaxTaps, radius + 3 * s, ws, L, st, &tpx);
         if (rc != M16_OK) return rc;
         if (c >= 0.f) {
-            fr_conv_x_eig_kernel<true><<<grid, block, 0, st>>>(a, tpx);
+            launch_x_eig<true>(a, tpx, grid, st);
         } else {
             a.c_dev = cdev + s;
-            fr_conv_x_eig_kernel<false><<<grid, block, 0, st>>>(a, tpx);
+            launch_x_eig<false>(a, tpx, grid, st);
             fr_c_kernel<<<1, 256, 0, st>>>(a.partials, L.nparts, cdev + s);
             fr_update_kernel<<<blocks1d, 256, 0, st>>>(a, n);
         }
