@@ -146,7 +146,15 @@ __device__ __forceinline__ void squeeze_last(const float q[4], float v[3])
     v[2] = c2 ? (-at2 + v[0] * (c1 ? -1.f : 1.f)) : at2;
 }
 
-__device__ __forceinline__ void eig3(const float h[6], float out[6])
+// state of one eigensolve between its sweeps and its sort
+struct Jacobi {
+    float on[3], off[3], oq[4];
+    bool converged;
+};
+
+// the cyclic sweeps, up to 50, until the off-diagonal sum is at most
+// max |h| * FLT_EPSILON (qeigs.cl:146-256)
+__device__ __forceinline__ void jacobi_sweeps(const float h[6], Jacobi &J)
 {
     const float GAMMA = 5.8284271247461900976f, C_STAR = 0.9238795325112867561f, S_STAR = 0.3826834323650897717f;
     float on[3] = {h[0], h[1], h[2]};
@@ -154,31 +162,11 @@ __device__ __forceinline__ void eig3(const float h[6], float out[6])
     float oq[4] = {0.f, 0.f, 0.f, 1.f};
     const float tol = fmaxf(fmaxf(fmaxf(fabsf(on[0]), fabsf(on[1])), fmaxf(fabsf(on[2]), fabsf(off[0]))),
                             fmaxf(fabsf(off[1]), fabsf(off[2]))) * FLT_EPSILON;
+    bool converged = false;
     for (int it = 0; it < 50; ++it) {
         if (fabsf(off[0]) + fabsf(off[1]) + fabsf(off[2]) <= tol) {
-            // sortEigs (qeigs.cl:60-92)
-            int o0, o1, o2, ot;
-            float vt;
-            bool c = eigcmp(on[0], on[1]);
-            vt = on[0]; on[0] = c ? on[0] : on[1]; o0 = c ? 0 : 1; on[1] = c ? on[1] : vt; o1 = c ? 1 : 0;
-            c = eigcmp(on[1], on[2]);
-            vt = on[1]; ot = o1; on[1] = c ? on[1] : on[2]; o1 = c ? o1 : 2; on[2] = c ? on[2] : vt; o2 = c ? 2 : ot;
-            c = eigcmp(on[0], on[1]);
-            vt = on[0]; ot = o0; on[0] = c ? on[0] : on[1]; o0 = c ? o0 : o1; on[1] = c ? on[1] : vt; o1 = c ? o1 : ot;
-            const int sk = (o0 << 1) | (o1 > o2 ? 1 : 0);
-            const float l0 = kSorterQuat[sk][0], l1 = kSorterQuat[sk][1], l2 = kSorterQuat[sk][2],
-                        l3 = kSorterQuat[sk][3];
-            float q[4];
-            q[3] = l3 * oq[3] - (l0 * oq[0] + l1 * oq[1] + l2 * oq[2]);
-            q[0] = l3 * oq[0] + l0 * oq[3] + l1 * oq[2] - l2 * oq[1];
-            q[1] = l3 * oq[1] - l0 * oq[2] + l1 * oq[3] + l2 * oq[0];
-            q[2] = l3 * oq[2] + l0 * oq[1] - l1 * oq[0] + l2 * oq[3];
-            q[3] = -q[3];   // eigenvectors in columns
-            float sq[3];
-            squeeze_last(q, sq);
-            out[0] = on[0]; out[1] = on[1]; out[2] = on[2];
-            out[3] = sq[0]; out[4] = sq[1]; out[5] = sq[2];
-            return;
+            converged = true;
+            break;
         }
 #pragma unroll
         for (int pq = 0; pq < 3; ++pq) {
@@ -215,7 +203,52 @@ __device__ __forceinline__ void eig3(const float h[6], float out[6])
             off[p] = c * off[p] + s * t2;
         }
     }
-    for (int k = 0; k < 6; ++k) out[k] = NAN;
+    for (int k = 0; k < 3; ++k) {
+        J.on[k] = on[k];
+        J.off[k] = off[k];
+    }
+    for (int k = 0; k < 4; ++k) J.oq[k] = oq[k];
+    J.converged = converged;
+}
+
+// eigenvalues ascending by |lambda| and the squeezed quaternion of the
+// eigenvectors (sortEigs, qeigs.cl:60-92, and the quaternion's squeeze);
+// NaN where the sweeps did not converge
+__device__ __forceinline__ void jacobi_finish(const Jacobi &J, float out[6])
+{
+    if (!J.converged) {
+        for (int k = 0; k < 6; ++k) out[k] = NAN;
+        return;
+    }
+    float on[3] = {J.on[0], J.on[1], J.on[2]};
+    const float *oq = J.oq;
+    int o0, o1, o2, ot;
+    float vt;
+    bool c = eigcmp(on[0], on[1]);
+    vt = on[0]; on[0] = c ? on[0] : on[1]; o0 = c ? 0 : 1; on[1] = c ? on[1] : vt; o1 = c ? 1 : 0;
+    c = eigcmp(on[1], on[2]);
+    vt = on[1]; ot = o1; on[1] = c ? on[1] : on[2]; o1 = c ? o1 : 2; on[2] = c ? on[2] : vt; o2 = c ? 2 : ot;
+    c = eigcmp(on[0], on[1]);
+    vt = on[0]; ot = o0; on[0] = c ? on[0] : on[1]; o0 = c ? o0 : o1; on[1] = c ? on[1] : vt; o1 = c ? o1 : ot;
+    const int sk = (o0 << 1) | (o1 > o2 ? 1 : 0);
+    const float l0 = kSorterQuat[sk][0], l1 = kSorterQuat[sk][1], l2 = kSorterQuat[sk][2], l3 = kSorterQuat[sk][3];
+    float q[4];
+    q[3] = l3 * oq[3] - (l0 * oq[0] + l1 * oq[1] + l2 * oq[2]);
+    q[0] = l3 * oq[0] + l0 * oq[3] + l1 * oq[2] - l2 * oq[1];
+    q[1] = l3 * oq[1] - l0 * oq[2] + l1 * oq[3] + l2 * oq[0];
+    q[2] = l3 * oq[2] + l0 * oq[1] - l1 * oq[0] + l2 * oq[3];
+    q[3] = -q[3];   // eigenvectors in columns
+    float sq[3];
+    squeeze_last(q, sq);
+    out[0] = on[0]; out[1] = on[1]; out[2] = on[2];
+    out[3] = sq[0]; out[4] = sq[1]; out[5] = sq[2];
+}
+
+__device__ __forceinline__ void eig3(const float h[6], float out[6])
+{
+    Jacobi J;
+    jacobi_sweeps(h, J);
+    jacobi_finish(J, out);
 }
 
 // Frangi response of one eigen-triple (frangi.cl:46-92)
@@ -250,10 +283,8 @@ struct FrArgs {
 // when c is given, else the eigen-triple stored for the update after c is
 // known, its norm folded into mx (calculateNorm, frangi.cl)
 template <bool FUSED_UPDATE>
-__device__ __forceinline__ void x_epilogue(const FrArgs &a, const float h[6], int64_t i, float &mx)
+__device__ __forceinline__ void x_output(const FrArgs &a, const float e[6], int64_t i, float &mx)
 {
-    float e[6];
-    eig3(h, e);
     if (FUSED_UPDATE) {
         const float v = vesselness(e, a.alpha, a.beta, a.c, a.bright != 0);
         if (v > a.val[i]) {
@@ -270,6 +301,14 @@ __device__ __forceinline__ void x_epilogue(const FrArgs &a, const float h[6], in
         // calculateNorm + redMax (NaN-neutral)
         mx = fmaxf(mx, sqrtf(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]));
     }
+}
+
+template <bool FUSED_UPDATE>
+__device__ __forceinline__ void x_epilogue(const FrArgs &a, const float h[6], int64_t i, float &mx)
+{
+    float e[6];
+    eig3(h, e);
+    x_output<FUSED_UPDATE>(a, e, i, mx);
 }
 
 // block maximum of the norms into the block's partial (redMax, max.cl);
@@ -494,7 +533,18 @@ __global__ void __launch_bounds__(kBX * kBY) fr_conv_x_eig_run_kernel(FrArgs a, 
                 h[5] = fmaf(tp.t[1][k], buf[5][lane + j], h[5]);
             }
             __syncwarp();
-            if (x < a.d2) x_epilogue<FUSED_UPDATE>(a, h, row + x, mx);
+            // Every lane solves (a zero matrix past the volume's edge), and the
+            // warp meets again before the sort and squeeze: without that, lanes
+            // that finish their sweeps at different counts run the squeeze's
+            // atan2/acos in as many separate groups (about 3x its instructions).
+            if (x >= a.d2)
+                for (int c = 0; c < 6; ++c) h[c] = 0.f;
+            Jacobi J;
+            jacobi_sweeps(h, J);
+            __syncwarp();
+            float e[6];
+            jacobi_finish(J, e);
+            if (x < a.d2) x_output<FUSED_UPDATE>(a, e, row + x, mx);
         }
     }
     if (!FUSED_UPDATE) block_max_to_partial(mx, red, a.partials);
