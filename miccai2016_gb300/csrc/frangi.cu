@@ -276,25 +276,51 @@ struct FrArgs {
     float *eig6;            // N x 6, or null when the update is fused
     float *val, *quat3;
     float *partials;        // per-block max Hessian norm
-    const float *c_dev;
+    const float *c_dev;     // the update kernel's scale's c
+    // c of the previous scale when its update rides along in this x pass
+    // (read from eig6 just before this scale's triple replaces it), else null
+    const float *c_prev;
+    int first;              // the update done here is the first one: it writes
+                            // val and quat without reading them
 };
 
-// eigensolve of one Hessian and its output: the running maximum update
-// when c is given, else the eigen-triple stored for the update after c is
-// known, its norm folded into mx (calculateNorm, frangi.cl)
+// one scale's update of the running maximum (updateVesselness,
+// frangi.cl:46-92).  The first update writes what the maximum over
+// (-inf, zero quaternion) and this scale gives: v where v is a number, the
+// initial values where it is NaN.
+__device__ __forceinline__ void update_max(const FrArgs &a, const float e[6], float c, bool first, int64_t i)
+{
+    const float v = vesselness(e, a.alpha, a.beta, c, a.bright != 0);
+    if (first) {
+        const bool take = v > -INFINITY;
+        a.val[i] = take ? v : -INFINITY;
+        a.quat3[3 * i] = take ? e[3] : 0.f;
+        a.quat3[3 * i + 1] = take ? e[4] : 0.f;
+        a.quat3[3 * i + 2] = take ? e[5] : 0.f;
+    } else if (v > a.val[i]) {
+        a.val[i] = v;
+        a.quat3[3 * i] = e[3];
+        a.quat3[3 * i + 1] = e[4];
+        a.quat3[3 * i + 2] = e[5];
+    }
+}
+
+// output of one eigensolve: the running maximum update when c is given,
+// else the eigen-triple stored for the update after c is known (first the
+// previous scale's triple there goes through its update, when c_prev is
+// set), its norm folded into mx (calculateNorm, frangi.cl)
 template <bool FUSED_UPDATE>
-__device__ __forceinline__ void x_output(const FrArgs &a, const float e[6], int64_t i, float &mx)
+__device__ __forceinline__ void x_output(const FrArgs &a, const float e[6], int64_t i, float c_prev, float &mx)
 {
     if (FUSED_UPDATE) {
-        const float v = vesselness(e, a.alpha, a.beta, a.c, a.bright != 0);
-        if (v > a.val[i]) {
-            a.val[i] = v;
-            a.quat3[3 * i] = e[3];
-            a.quat3[3 * i + 1] = e[4];
-            a.quat3[3 * i + 2] = e[5];
-        }
+        update_max(a, e, a.c, a.first != 0, i);
     } else {
         float2 *o = reinterpret_cast<float2 *>(a.eig6 + 6 * i);
+        if (a.c_prev) {
+            const float2 p01 = o[0], p23 = o[1], p45 = o[2];
+            const float ep[6] = {p01.x, p01.y, p23.x, p23.y, p45.x, p45.y};
+            update_max(a, ep, c_prev, a.first != 0, i);
+        }
         o[0] = make_float2(e[0], e[1]);
         o[1] = make_float2(e[2], e[3]);
         o[2] = make_float2(e[4], e[5]);
@@ -304,11 +330,11 @@ __device__ __forceinline__ void x_output(const FrArgs &a, const float e[6], int6
 }
 
 template <bool FUSED_UPDATE>
-__device__ __forceinline__ void x_epilogue(const FrArgs &a, const float h[6], int64_t i, float &mx)
+__device__ __forceinline__ void x_epilogue(const FrArgs &a, const float h[6], int64_t i, float c_prev, float &mx)
 {
     float e[6];
     eig3(h, e);
-    x_output<FUSED_UPDATE>(a, e, i, mx);
+    x_output<FUSED_UPDATE>(a, e, i, c_prev, mx);
 }
 
 // block maximum of the norms into the block's partial (redMax, max.cl);
@@ -341,6 +367,7 @@ __global__ void __launch_bounds__(kBX * kBY) fr_conv_x_eig_kernel(FrArgs a, Axis
     __shared__ float red[32];
     const int x = blockIdx.x * kBX + threadIdx.x;
     const int y = blockIdx.y * kBY + threadIdx.y;
+    const float c_prev = (!FUSED_UPDATE && a.c_prev) ? *a.c_prev : 0.f;
     float mx = -INFINITY;
     if (x < a.d2 && y < a.d1) {
         const int za = blockIdx.z * a.zc, zb = min(za + a.zc, a.d0);
@@ -362,7 +389,7 @@ __global__ void __launch_bounds__(kBX * kBY) fr_conv_x_eig_kernel(FrArgs a, Axis
                 h[4] = fmaf(t1, __ldg(a.six + 4 * n + idx), h[4]);
                 h[5] = fmaf(t1, __ldg(a.six + 5 * n + idx), h[5]);
             }
-            x_epilogue<FUSED_UPDATE>(a, h, row + x, mx);
+            x_epilogue<FUSED_UPDATE>(a, h, row + x, c_prev, mx);
         }
     }
     if (!FUSED_UPDATE) block_max_to_partial(mx, red, a.partials);
@@ -502,6 +529,7 @@ __global__ void __launch_bounds__(kBX * kBY) fr_conv_x_eig_run_kernel(FrArgs a, 
     const int lane = threadIdx.x;
     const int x0 = blockIdx.x * kBX, x = x0 + lane;
     const int y = blockIdx.y * kBY + threadIdx.y;
+    const float c_prev = (!FUSED_UPDATE && a.c_prev) ? *a.c_prev : 0.f;
     float mx = -INFINITY;
     if (y < a.d1) {   // uniform over the warp
         float (*buf)[W] = rows[threadIdx.y];
@@ -544,7 +572,7 @@ __global__ void __launch_bounds__(kBX * kBY) fr_conv_x_eig_run_kernel(FrArgs a, 
             __syncwarp();
             float e[6];
             jacobi_finish(J, e);
-            if (x < a.d2) x_output<FUSED_UPDATE>(a, e, row + x, mx);
+            if (x < a.d2) x_output<FUSED_UPDATE>(a, e, row + x, c_prev, mx);
         }
     }
     if (!FUSED_UPDATE) block_max_to_partial(mx, red, a.partials);
@@ -585,31 +613,18 @@ __global__ void fr_c_kernel(const float *__restrict__ part, int nparts, float *c
     if (threadIdx.x == 0) *c_out = 0.5f * (s[0] == -INFINITY ? NAN : s[0]);
 }
 
-// updateVesselness (frangi.cl:46-92) from the stored eigendecompositions
+// updateVesselness (frangi.cl:46-92) of the last scale from its stored
+// eigendecompositions (the earlier scales' updates ride along in the next
+// scale's x pass)
 __global__ void fr_update_kernel(FrArgs a, int64_t n)
 {
     const float c = *a.c_dev;
+    const bool first = a.first != 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float2 *p = reinterpret_cast<const float2 *>(a.eig6 + 6 * i);
         const float2 e01 = p[0], e23 = p[1], e45 = p[2];
         const float e[6] = {e01.x, e01.y, e23.x, e23.y, e45.x, e45.y};
-        const float v = vesselness(e, a.alpha, a.beta, c, a.bright != 0);
-        if (v > a.val[i]) {
-            a.val[i] = v;
-            a.quat3[3 * i] = e[3];
-            a.quat3[3 * i + 1] = e[4];
-            a.quat3[3 * i + 2] = e[5];
-        }
-    }
-}
-
-__global__ void fr_init_kernel(float *val, float *quat3, int64_t n)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        val[i] = -INFINITY;
-        quat3[3 * i] = 0.f;
-        quat3[3 * i + 1] = 0.f;
-        quat3[3 * i + 2] = 0.f;
+        update_max(a, e, c, first, i);
     }
 }
 
@@ -737,7 +752,6 @@ extern "C" int m16_frangi(const float *img, int32_t d0, int32_t d1, int32_t d2, 
     char *ws = (char *)workspace;
     const int64_t n = (int64_t)d0 * d1 * d2;
     const int blocks1d = (int)std::min<int64_t>(8 * kSMs, div_up(n, 256));
-    fr_init_kernel<<<blocks1d, 256, 0, st>>>(val, quat3, n);
     FrArgs a;
     a.d0 = d0; a.d1 = d1; a.d2 = d2; a.zc = fr_zc(d0, d1, d2);
     a.alpha = alpha; a.beta = beta; a.c = c; a.bright = bright;
@@ -745,6 +759,9 @@ extern "C" int m16_frangi(const float *img, int32_t d0, int32_t d1, int32_t d2, 
     a.eig6 = (float *)(ws + L.eig);
     a.val = val; a.quat3 = quat3;
     a.partials = (float *)(ws + L.part);
+    a.c_dev = nullptr;
+    a.c_prev = nullptr;
+    a.first = 0;
     float *cdev = (float *)(ws + L.cdev);
     const dim3 grid((unsigned)div_up(d2, kBX), (unsigned)div_up(d1, kBY), (unsigned)div_up(d0, a.zc));
     for (int s = 0; s < nscales; ++s) {
@@ -752,13 +769,23 @@ extern "C" int m16_frangi(const float *img, int32_t d0, int32_t d1, int32_t d2, 
         const int rc = hessian_passes(img, d0, d1, d2, taps + (size_t)s * 9 * kMaxTaps, radius + 3 * s, ws, L, st, &tpx);
         if (rc != M16_OK) return rc;
         if (c >= 0.f) {
+            a.first = s == 0;
             launch_x_eig<true>(a, tpx, grid, st);
         } else {
-            a.c_dev = cdev + s;
+            // scale s - 1's update rides along: its triple is read at each
+            // voxel just before scale s's replaces it
+            a.c_prev = s > 0 ? cdev + s - 1 : nullptr;
+            a.first = s == 1;
             launch_x_eig<false>(a, tpx, grid, st);
             fr_c_kernel<<<1, 256, 0, st>>>(a.partials, L.nparts, cdev + s);
-            fr_update_kernel<<<blocks1d, 256, 0, st>>>(a, n);
         }
+        M16_CUDA_TRY(cudaGetLastError());
+    }
+    if (c < 0.f) {
+        a.c_dev = cdev + nscales - 1;
+        a.c_prev = nullptr;
+        a.first = nscales == 1;
+        fr_update_kernel<<<blocks1d, 256, 0, st>>>(a, n);
         M16_CUDA_TRY(cudaGetLastError());
     }
     if (c_used) {
