@@ -106,6 +106,7 @@ __global__ void __launch_bounds__(kBX * kBY) dr_detect_ridges_kernel(const float
     }
     const float pos[3] = {(float)z, (float)y, (float)x};
     const int dims[3] = {d0, d1, d2};
+    const int64_t s0 = (int64_t)d1 * d2;
     float maxv = -INFINITY;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
@@ -119,17 +120,34 @@ __global__ void __launch_bounds__(kBX * kBY) dr_detect_ridges_kernel(const float
             o[k] = (int)p[k];   // toward zero, as convert_int3
             p[k] = __fsub_rn(p[k], (float)o[k]);
         }
+        const float u[3] = {__fsub_rn(1.f, p[0]), __fsub_rn(1.f, p[1]), __fsub_rn(1.f, p[2])};
         float v = 0.f;
+        // all eight corners inside the volume (one test per sample instead of
+        // one per corner; o < dims - 1 also holds off a saturated conversion)
+        if (o[0] >= 0 && o[1] >= 0 && o[2] >= 0 && o[0] < d0 - 1 && o[1] < d1 - 1 && o[2] < d2 - 1) {
+            const float *base = resp + ((int64_t)o[0] * d1 + o[1]) * d2 + o[2];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int r0 = k >> 2, r1 = (k >> 1) & 1, r2 = k & 1;
-            const int a0 = o[0] + r0, a1 = o[1] + r1, a2 = o[2] + r2;
-            const float w0 = r0 ? p[0] : __fsub_rn(1.f, p[0]);
-            const float w1 = r1 ? p[1] : __fsub_rn(1.f, p[1]);
-            const float w2 = r2 ? p[2] : __fsub_rn(1.f, p[2]);
-            const bool out = a0 < 0 || a1 < 0 || a2 < 0 || a0 >= dims[0] || a1 >= dims[1] || a2 >= dims[2];
-            const float s = out ? -1.f : __ldg(resp + ((int64_t)a0 * d1 + a1) * d2 + a2);
-            v = __fadd_rn(v, __fmul_rn(__fmul_rn(__fmul_rn(s, w0), w1), w2));
+            for (int k = 0; k < 8; ++k) {
+                const int r0 = k >> 2, r1 = (k >> 1) & 1, r2 = k & 1;
+                const float w0 = r0 ? p[0] : u[0];
+                const float w1 = r1 ? p[1] : u[1];
+                const float w2 = r2 ? p[2] : u[2];
+                const float s = __ldg(base + (r0 ? s0 : 0) + (r1 ? d2 : 0) + r2);
+                v = __fadd_rn(v, __fmul_rn(__fmul_rn(__fmul_rn(s, w0), w1), w2));
+            }
+        } else {
+            // corners outside the volume read -1 (detect_ridges.cl)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int r0 = k >> 2, r1 = (k >> 1) & 1, r2 = k & 1;
+                const int a0 = o[0] + r0, a1 = o[1] + r1, a2 = o[2] + r2;
+                const float w0 = r0 ? p[0] : u[0];
+                const float w1 = r1 ? p[1] : u[1];
+                const float w2 = r2 ? p[2] : u[2];
+                const bool out = a0 < 0 || a1 < 0 || a2 < 0 || a0 >= dims[0] || a1 >= dims[1] || a2 >= dims[2];
+                const float s = out ? -1.f : __ldg(resp + ((int64_t)a0 * d1 + a1) * d2 + a2);
+                v = __fadd_rn(v, __fmul_rn(__fmul_rn(__fmul_rn(s, w0), w1), w2));
+            }
         }
         maxv = v > maxv ? v : maxv;
     }
@@ -165,7 +183,11 @@ __device__ __forceinline__ float rsqrt_ref(float x) { return __fdiv_rn(1.f, __fs
 
 // qsqueeze (quaternion_math.h:20-39), scalar part first, written literally
 // (products with the 0/1 conditions included: they decide the sign of zero
-// that atan2 sees)
+// that atan2 sees).  The reference forms v[1] and atan2's denominator in
+// double: (pi or 0) * f2 + ac * nf2 and (0.5 - x) * f2 + y * nf2.  One of
+// f2, nf2 is zero, so one term is +-0 (or NaN) and the sum is the other
+// term, with the same sign-of-zero rules in float; 0.5 - x rounded from
+// double is the float difference (Figueroa 1995).  Float gives the same bits.
 __device__ __forceinline__ void qsqueeze_ref(const float q[4], float v[3])
 {
     const float q1spq2s = __fadd_rn(sq_rn(q[1]), sq_rn(q[2]));
@@ -174,17 +196,16 @@ __device__ __forceinline__ void qsqueeze_ref(const float q[4], float v[3])
     const float f2 = c2 ? 1.f : 0.f, nf2 = c2 ? 0.f : 1.f;
     const float q1q3 = __fmul_rn(q[1], q[3]), q2q0 = __fmul_rn(q[2], q[0]);
     const float q1q0 = __fmul_rn(q[1], q[0]), q2q3 = __fmul_rn(q[2], q[3]);
-    auto satan2 = [](double a, double b) {
-        return (a == 0.0 && b == 0.0) ? 0.f : atan2f((float)a, (float)b);
-    };
+    auto satan2 = [](float a, float b) { return (a == 0.f && b == 0.f) ? 0.f : atan2f(a, b); };
     v[0] = satan2(__fadd_rn(q1q3, q2q0), __fsub_rn(q1q0, q2q3));
     const float ac = acosf(fminf(fmaxf(__fsub_rn(1.f, __fmul_rn(2.f, q1spq2s)), -1.f), 1.f));
-    v[1] = (float)((c1 ? 0.0 : 3.14159265358979323846) * (double)f2 + (double)__fmul_rn(ac, nf2));
+    const float pi_f = 3.14159265358979323846f;   // float nearest to pi, as (float) of the double
+    v[1] = __fadd_rn(__fmul_rn(c1 ? 0.f : pi_f, f2), __fmul_rn(ac, nf2));
     float at2 = __fadd_rn(__fmul_rn(__fsub_rn(__fmul_rn(q[1], q[2]), __fmul_rn(q[0], q[3])), f2),
                           __fmul_rn(__fsub_rn(q1q3, q2q0), nf2));
-    const double den = (0.5 - (double)__fadd_rn(sq_rn(q[2]), sq_rn(q[3]))) * (double)f2 +
-                       (double)__fmul_rn(__fadd_rn(q1q0, q2q3), nf2);
-    at2 = satan2((double)at2, den);
+    const float den = __fadd_rn(__fmul_rn(__fsub_rn(0.5f, __fadd_rn(sq_rn(q[2]), sq_rn(q[3]))), f2),
+                                __fmul_rn(__fadd_rn(q1q0, q2q3), nf2));
+    at2 = satan2(at2, den);
     v[2] = __fadd_rn(__fmul_rn(__fadd_rn(-at2, __fmul_rn(v[0], c1 ? -1.f : 1.f)), f2), __fmul_rn(at2, nf2));
 }
 
@@ -204,32 +225,37 @@ __global__ void dr_complete_kernel(const float *in3, float *out3, int64_t n)
         const float m00 = e0[0], m01 = e1[0], m02 = e2[0];
         const float m10 = e0[1], m11 = e1[1], m12 = e2[1];
         const float m20 = e0[2], m21 = e1[2], m22 = e2[2];
+        // The reference rounds s + 1, r * 0.5 and 0.25 / s from double.  Each
+        // is one operation on floats, and a double result rounded to float is
+        // the correctly rounded float result (53 >= 2 * 24 + 2 bits, Figueroa
+        // 1995), so the float operations below give the same bits.  Only
+        // 1 + m00 - m11 - m22 (three roundings) stays in double.
         float q[4];
         float s = __fadd_rn(__fadd_rn(m00, m11), m22);
         if (s > 0.f) {
-            s = (float)((double)rsqrt_ref((float)((double)s + 1.0)) * 0.5);
-            q[0] = (float)(0.25 / (double)s);
+            s = __fmul_rn(rsqrt_ref(__fadd_rn(s, 1.f)), 0.5f);
+            q[0] = __fdiv_rn(0.25f, s);
             q[1] = __fmul_rn(__fsub_rn(m21, m12), s);
             q[2] = __fmul_rn(__fsub_rn(m02, m20), s);
             q[3] = __fmul_rn(__fsub_rn(m10, m01), s);
         } else if (m00 > m11 && m00 > m22) {
-            s = (float)((double)rsqrt_ref((float)(1.0 + (double)m00 - (double)m11 - (double)m22)) * 0.5);
+            s = __fmul_rn(rsqrt_ref((float)(1.0 + (double)m00 - (double)m11 - (double)m22)), 0.5f);
             q[0] = __fmul_rn(__fsub_rn(m21, m12), s);
-            q[1] = (float)(0.25 / (double)s);
+            q[1] = __fdiv_rn(0.25f, s);
             q[2] = __fmul_rn(__fadd_rn(m01, m10), s);
             q[3] = __fmul_rn(__fadd_rn(m02, m20), s);
         } else if (m11 > m22) {
-            s = (float)((double)rsqrt_ref((float)(1.0 + (double)m11 - (double)m00 - (double)m22)) * 0.5);
+            s = __fmul_rn(rsqrt_ref((float)(1.0 + (double)m11 - (double)m00 - (double)m22)), 0.5f);
             q[0] = __fmul_rn(__fsub_rn(m02, m20), s);
             q[1] = __fmul_rn(__fadd_rn(m01, m10), s);
-            q[2] = (float)(0.25 / (double)s);
+            q[2] = __fdiv_rn(0.25f, s);
             q[3] = __fmul_rn(__fadd_rn(m12, m21), s);
         } else {
-            s = (float)((double)rsqrt_ref((float)(1.0 + (double)m22 - (double)m00 - (double)m11)) * 0.5);
+            s = __fmul_rn(rsqrt_ref((float)(1.0 + (double)m22 - (double)m00 - (double)m11)), 0.5f);
             q[0] = __fmul_rn(__fsub_rn(m10, m01), s);
             q[1] = __fmul_rn(__fadd_rn(m02, m20), s);
             q[2] = __fmul_rn(__fadd_rn(m12, m21), s);
-            q[3] = (float)(0.25 / (double)s);
+            q[3] = __fdiv_rn(0.25f, s);
         }
         float sq[3];
         qsqueeze_ref(q, sq);
