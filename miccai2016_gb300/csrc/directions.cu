@@ -181,6 +181,27 @@ __device__ __forceinline__ void normalize3(const float v[3], float o[3])
 
 __device__ __forceinline__ float rsqrt_ref(float x) { return __fdiv_rn(1.f, __fsqrt_rn(x)); }
 
+// (float)(1.0 + (double)a - (double)b - (double)c), the reference's rounding
+// of mat2quat's diagonal sums.  When every nonzero term is finite with
+// 2^-27 <= |t| < 2, each term is a multiple of 2^-50 and every partial sum
+// is below 8 in magnitude, so all three double additions are exact and the
+// result is the correctly rounded float of the exact sum: here in 64-bit
+// integers scaled by 2^50, rounded once by the integer-to-float conversion.
+// Other terms (tiny, NaN, infinite) take the double path.
+__device__ __forceinline__ float one_plus_minus_minus(float a, float b, float c)
+{
+    const float lo = 7.450580596923828125e-9f;   // 2^-27
+    auto exact = [lo](float t) { return t == 0.f || (fabsf(t) >= lo && fabsf(t) < 2.f); };
+    if (exact(a) && exact(b) && exact(c)) {
+        const float up = 1125899906842624.f;           // 2^50
+        const float down = 8.8817841970012523e-16f;    // 2^-50
+        const long long sum = (1LL << 50) + __float2ll_rn(__fmul_rn(a, up)) - __float2ll_rn(__fmul_rn(b, up)) -
+                              __float2ll_rn(__fmul_rn(c, up));
+        return __fmul_rn(__ll2float_rn(sum), down);
+    }
+    return (float)(1.0 + (double)a - (double)b - (double)c);
+}
+
 // qsqueeze (quaternion_math.h:20-39), scalar part first, written literally
 // (products with the 0/1 conditions included: they decide the sign of zero
 // that atan2 sees).  The reference forms v[1] and atan2's denominator in
@@ -228,8 +249,8 @@ __global__ void dr_complete_kernel(const float *in3, float *out3, int64_t n)
         // The reference rounds s + 1, r * 0.5 and 0.25 / s from double.  Each
         // is one operation on floats, and a double result rounded to float is
         // the correctly rounded float result (53 >= 2 * 24 + 2 bits, Figueroa
-        // 1995), so the float operations below give the same bits.  Only
-        // 1 + m00 - m11 - m22 (three roundings) stays in double.
+        // 1995), so the float operations below give the same bits; the
+        // diagonal sums go through one_plus_minus_minus.
         float q[4];
         float s = __fadd_rn(__fadd_rn(m00, m11), m22);
         if (s > 0.f) {
@@ -239,19 +260,19 @@ __global__ void dr_complete_kernel(const float *in3, float *out3, int64_t n)
             q[2] = __fmul_rn(__fsub_rn(m02, m20), s);
             q[3] = __fmul_rn(__fsub_rn(m10, m01), s);
         } else if (m00 > m11 && m00 > m22) {
-            s = __fmul_rn(rsqrt_ref((float)(1.0 + (double)m00 - (double)m11 - (double)m22)), 0.5f);
+            s = __fmul_rn(rsqrt_ref(one_plus_minus_minus(m00, m11, m22)), 0.5f);
             q[0] = __fmul_rn(__fsub_rn(m21, m12), s);
             q[1] = __fdiv_rn(0.25f, s);
             q[2] = __fmul_rn(__fadd_rn(m01, m10), s);
             q[3] = __fmul_rn(__fadd_rn(m02, m20), s);
         } else if (m11 > m22) {
-            s = __fmul_rn(rsqrt_ref((float)(1.0 + (double)m11 - (double)m00 - (double)m22)), 0.5f);
+            s = __fmul_rn(rsqrt_ref(one_plus_minus_minus(m11, m00, m22)), 0.5f);
             q[0] = __fmul_rn(__fsub_rn(m02, m20), s);
             q[1] = __fmul_rn(__fadd_rn(m01, m10), s);
             q[2] = __fdiv_rn(0.25f, s);
             q[3] = __fmul_rn(__fadd_rn(m12, m21), s);
         } else {
-            s = __fmul_rn(rsqrt_ref((float)(1.0 + (double)m22 - (double)m00 - (double)m11)), 0.5f);
+            s = __fmul_rn(rsqrt_ref(one_plus_minus_minus(m22, m00, m11)), 0.5f);
             q[0] = __fmul_rn(__fsub_rn(m10, m01), s);
             q[1] = __fmul_rn(__fadd_rn(m02, m20), s);
             q[2] = __fmul_rn(__fadd_rn(m12, m21), s);
