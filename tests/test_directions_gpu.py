@@ -218,6 +218,28 @@ def test_ridge_detection_only_and_no_cleaning():
     assert np.mean(obj.ridge != O.detect_ridges(resp, quat, 0.3)) <= 1e-4
 
 
+def test_completion_of_near_axis_directions_matches_the_oracle():
+    # Near-axis directions give diagonal terms around and far below 2^-27:
+    # mat2quat's 1 + m00 - m11 - m22 takes the exact integer sum above that
+    # size and the double expression below it.  Rotations within 1e-5 of the
+    # oracle's (the squeeze's atan2/acos differ in the last bits between libm
+    # and CUDA), with the main direction kept.
+    from miccai2016_gb300.adjust_directions import TransformationCompleter
+    rng = np.random.RandomState(27)
+    vs = []
+    for t in (1e-12, 1e-9, 7.450580596923828125e-9, 7.5e-9, 3e-8, 1e-6, 2.0 ** -26, 2.0 ** -28):
+        for sgn in ((1, 1, 1), (1, -1, 1), (-1, 1, -1), (-1, -1, -1)):
+            for perm in ((0, 1, 2), (1, 2, 0), (2, 0, 1), (0, 2, 1), (1, 0, 2), (2, 1, 0)):
+                vs.append((np.array([1.0, t, 0.37 * t])[list(perm)] * np.array(sgn)))
+    v = np.concatenate([np.array(vs), rng.normal(size=(4000, 3)) * np.array([1, 1e-8, 1e-8]),
+                        rng.normal(size=(4000, 3)) * np.array([1e-9, 1, 1e-7])]).astype(np.float32)
+    v = v[:8000].reshape(20, 20, 20, 3)
+    q = TransformationCompleter(v).complete()
+    assert np.max(np.abs(_rot(q) - _rot(O.complete_transformations(v)))) <= 1e-5
+    vn = v / np.linalg.norm(v.astype(np.float64), axis=-1, keepdims=True)
+    assert np.max(np.abs(_gpu_extract(q) - vn)) <= 1e-5
+
+
 def test_completer_round_trip_keeps_the_main_direction():
     from miccai2016_gb300.adjust_directions import TransformationCompleter
     rng = np.random.RandomState(9)

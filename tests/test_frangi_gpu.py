@@ -41,8 +41,11 @@ def _rot(sq):
                      2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1).reshape(-1, 3, 3)
 
 
+# radius round(4 sigma): 4.4 gives 18, beyond the passes instantiated per
+# radius (1-16), so the last case runs the kernels for any radius
 @pytest.mark.parametrize("shape,sigma", [((20, 24, 28), (1.0, 1.0, 1.0)), ((33, 17, 40), (3.0, 2.0, 2.5)),
-                                         ((5, 70, 9), (1.5, 1.5, 1.5)), ((1, 12, 13), (1.0, 1.0, 1.0))])
+                                         ((5, 70, 9), (1.5, 1.5, 1.5)), ((1, 12, 13), (1.0, 1.0, 1.0)),
+                                         ((24, 20, 40), (4.4, 4.4, 4.4))])
 def test_hessian_matches_oracle(shape, sigma):
     from miccai2016_gb300.qfrangi_gpu import hessian
     rng = np.random.RandomState(sum(shape))
