@@ -515,12 +515,24 @@ __device__ __forceinline__ float axis_gap(int p, int lo, int hi, float s)
     return __fmul_rn((float)m, s);
 }
 
+// Each warp takes a kNrPX x kNrPY patch of the block's 32 x 8 tile (x, y),
+// so that its voxels fall into fewer cells and walk the same cells' point
+// lists together.  Measured on GB300 (256^3 helix, R = 1.9 M, 4^3 cells):
+// 32 x 1 2.28 ms, 16 x 2 2.19 ms, 8 x 4 2.29 ms, 4 x 8 2.30 ms.
+#ifndef M16_NR_PATCH
+#define M16_NR_PATCH 16
+#endif
+constexpr int kNrPX = M16_NR_PATCH, kNrPY = 32 / kNrPX;
+static_assert(kBX % kNrPX == 0 && kBY % kNrPY == 0 && (kBX / kNrPX) * (kBY / kNrPY) == kBY,
+              "a warp per patch, the block's 8 warps tiling 32 x 8");
+
 __global__ void __launch_bounds__(kBX * kBY) dr_adjust_indexed_kernel(
     float *__restrict__ dirs3, const float4 *__restrict__ pts, const unsigned *__restrict__ start,
     const float *__restrict__ rdirs, CellGrid g, int d0, int d1, int d2, float s0, float s1, float s2)
 {
-    const int x = blockIdx.x * kBX + threadIdx.x;
-    const int y = blockIdx.y * kBY + threadIdx.y;
+    const int w = threadIdx.y, lane = threadIdx.x;
+    const int x = blockIdx.x * kBX + (w % (kBX / kNrPX)) * kNrPX + lane % kNrPX;
+    const int y = blockIdx.y * kBY + (w / (kBX / kNrPX)) * kNrPY + lane / kNrPX;
     const int z = blockIdx.z;
     if (x >= d2 || y >= d1) return;
     const float p0 = (float)z, p1 = (float)y, p2 = (float)x;
