@@ -481,6 +481,20 @@ int m16_compose_signs(int64_t n, const int32_t *order, int64_t n_order, const in
                       int8_t *s);
 
 /*
+ * Host function (no device work): per segment label l (0 .. num_labels - 1)
+ * the sums over the points with point_label[i] == l (host int32,
+ * num_points) of dirs3[i][k] * voxel_size3[k] (dirs3 host float32,
+ * num_points x 3), taken in point order and in double, each product rounded
+ * before it is added; sums3 (host, num_labels x 3 doubles) is overwritten.
+ * The per-segment summed directions that the ridge cleaning of
+ * AdvancedAdjuster._do_clean_ridge (adjust_directions.py:319-337) ranks its
+ * segments by, with np.bincount's order and rounding.  A label outside
+ * 0 .. num_labels - 1 returns M16_ERR_BAD_ARG.
+ */
+int m16_segment_direction_sums(const int32_t *point_label, const float *dirs3, int64_t num_points,
+                               const double *voxel_size3, int32_t num_labels, double *sums3);
+
+/*
  * Host function (no device work): the visiting order of that propagation over
  * an undirected forest of n points (n_edges edges ea[k] -- eb[k], host):
  * breadth first from `root`, then every other tree from its lowest-index

@@ -129,6 +129,8 @@ def _declare(L):
     L.m16_tree_order.argtypes = [_i64, _vp, _vp, _i64, _i32, _vp, _vp]
     L.m16_compose_signs.restype = ctypes.c_int
     L.m16_compose_signs.argtypes = [_i64, _vp, _i64, _vp, _vp, _vp]
+    L.m16_segment_direction_sums.restype = ctypes.c_int
+    L.m16_segment_direction_sums.argtypes = [_vp, _vp, _i64, _vp, _i32, _vp]
     L.m16_ridge_edge_codes.restype = ctypes.c_int
     L.m16_ridge_edge_codes.argtypes = [_vp, _i64, _vp, _vp, _i64, _vp, _vp]
     L.m16_ridge_signs_workspace_bytes.restype = ctypes.c_size_t

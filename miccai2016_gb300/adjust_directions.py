@@ -247,7 +247,8 @@ class AdvancedAdjuster(TreePrintable):
         if len(coords) == 0:
             raise ValueError("no ridge points: nothing to propagate directions along")
         with self._timed("mst_local" if not join_components else "mst_local_and_joins"):
-            a, b = ridge_mst_edges(coords, self.voxel_size, join_components=join_components, local=self.mst_local)
+            a, b = ridge_mst_edges(coords, self.voxel_size, join_components=join_components, local=self.mst_local,
+                                   on_device=True)
         with self._timed("sign_propagation"):
             d_dirs = d_main[d_coords[:, 0], d_coords[:, 1], d_coords[:, 2]]
             adjusted = propagate_signs_device(d_dirs, a, b).cpu().numpy()
@@ -259,26 +260,46 @@ class AdvancedAdjuster(TreePrintable):
         segments selected on the device.  Returns the cleaned uint8 mask."""
         torch = N.torch_mod()
         coords, d_coords = pts
-        scaled = ridge_dirs * self.__voxel_size   # float32 * tuple -> float64, as in the reference
         with self._timed("clean_labels"):
             d_comp, n_lab = label_device(d_mask, 26)
             point_label = d_comp[d_coords[:, 0], d_coords[:, 1], d_coords[:, 2]].cpu().numpy()
         with self._timed("clean_segment_sums"):
-            kept = self._kept_segments(point_label, n_lab, len(coords) < d_mask.numel(), scaled)
+            sums = self._segment_sums(point_label, n_lab, ridge_dirs)
+            kept = self._kept_segments(n_lab, len(coords) < d_mask.numel(), sums)
         keep = np.zeros(n_lab + 1, dtype=np.uint8)
         keep[np.asarray(kept, dtype=np.int64)] = 1
         return torch.from_numpy(keep).to(N.device())[d_comp.long()]
 
-    def _kept_segments(self, point_label, n_lab, has_background, scaled):
+    def _segment_sums(self, point_label, n_lab, ridge_dirs):
+        """(n_lab + 1) x 3 float64: per label the directions of its ridge
+        points times the voxel size, summed in the C order of its voxels, one
+        after the other (np.sum over axis 0 of the reference's list; np.bincount
+        adds sequentially too).  The library's m16_segment_direction_sums does
+        it in one pass where the reference's product is a double one (float32
+        directions, a voxel size that numpy multiplies in double); otherwise
+        np.bincount."""
+        dirs = np.asarray(ridge_dirs)
+        vs = np.asarray(self.__voxel_size)
+        if (dirs.dtype == np.float32 and dirs.ndim == 2 and dirs.shape[1] == 3 and vs.dtype.kind in "iuf"
+                and np.result_type(dirs.dtype, vs.dtype) == np.float64):
+            dirs = np.ascontiguousarray(dirs)
+            pl = np.ascontiguousarray(point_label, dtype=np.int32)
+            v3 = np.ascontiguousarray(np.broadcast_to(vs.astype(np.float64), (3,)))
+            sums = np.empty((n_lab + 1, 3), np.float64)
+            vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+            N.check("m16_segment_direction_sums",
+                    N.lib().m16_segment_direction_sums(vp(pl), vp(dirs), len(pl), vp(v3), n_lab + 1, vp(sums)))
+            return sums
+        scaled = dirs * self.__voxel_size   # float32 * tuple -> float64, as in the reference
+        return np.stack([np.bincount(point_label, weights=scaled[:, k], minlength=n_lab + 1) for k in range(3)], -1)
+
+    def _kept_segments(self, n_lab, has_background, sums):
         """The labels the cleaning keeps (adjust_directions.py:319-337): the
         ceil(3 ln(e + n)) segments with the longest summed (scaled) direction,
-        the sort stable on ties.  Per segment the directions are summed in
-        the C order of its voxels, one after the other (np.sum over axis 0
-        of the reference's list, and np.bincount, add sequentially)."""
+        the sort stable on ties; sums from _segment_sums."""
         # np.unique(components)[1:] without the sort: the labels are 1..n_lab,
         # and "[1:]" drops label 1 too when no voxel is background
         labels = np.arange(1 if has_background else 2, n_lab + 1)
-        sums = np.stack([np.bincount(point_label, weights=scaled[:, k], minlength=n_lab + 1) for k in range(3)], -1)
         lengths = {}
         for lab in labels:
             lengths[lab] = np.linalg.norm(sums[lab])
@@ -327,12 +348,12 @@ class AdvancedAdjuster(TreePrintable):
         """Keep the ceil(3 ln(e + n)) 26-connected ridge segments whose summed
         directions are longest (adjust_directions.py:290-339).  Per segment the
         directions are summed in the reference's order (C order of the voxels)."""
-        scaled = ridge_dirs * self.__voxel_size   # float32 * tuple -> float64, as in the reference
         with self._timed("clean_labels"):
             components, n_lab = label26(labeled_ridge, where=self.labeler)
         with self._timed("clean_segment_sums"):
             point_label = components[tuple(np.asarray(ridge_coords, np.intp).T)]
-            kept = self._kept_segments(point_label, n_lab, len(ridge_coords) < components.size, scaled)
+            sums = self._segment_sums(point_label, n_lab, ridge_dirs)
+            kept = self._kept_segments(n_lab, len(ridge_coords) < components.size, sums)
         keep = np.zeros(n_lab + 1, dtype=bool)   # np.in1d(components, kept) as a table lookup
         keep[np.asarray(kept, dtype=np.int64)] = True
         cleaned = keep[components].astype(labeled_ridge.dtype).reshape(components.shape)

@@ -2,7 +2,10 @@
 Build recipe of the CUDA library: every csrc/*.cu translation unit is compiled
 for sm_103a with nvcc (in parallel) and linked into
 miccai2016_gb300/_lib/libmiccai2016_gb300.so, the C-ABI library declared in
-include/miccai2016_gb300.h.  No cmake, one -gencode, static cudart.
+include/miccai2016_gb300.h.  No cmake, one -gencode, static cudart.  The
+host-only csrc/*.cpp files go through nvcc as plain C++ with multiply-add
+contraction off (-ffp-contract=off): their floating-point sums must round
+each product as numpy does, on x86 and Arm hosts alike.
 """
 from __future__ import annotations
 
@@ -24,6 +27,7 @@ LIB_NAME = "libmiccai2016_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
+HOST_CPP_FLAGS = ["-O2", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off"]
 
 
 def nvcc_path() -> str:
@@ -44,7 +48,7 @@ def _headers():
 def build(force: bool = False, verbose: bool = False) -> str:
     """Compile (if stale) and return the path of the shared library."""
     os.makedirs(OBJ_DIR, exist_ok=True)
-    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu"))) + sorted(glob.glob(os.path.join(CSRC, "*.cpp")))
     if not srcs:
         raise RuntimeError("no CUDA sources under %s" % CSRC)
     out = lib_path()
@@ -56,7 +60,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if (not force and os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src)
                 and os.path.getmtime(obj) >= newest_hdr):
             return obj, False
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + EXTRA_DEFINES + ["-c", src, "-o", obj]
+        flags = HOST_CPP_FLAGS if src.endswith(".cpp") else ARCH + NVCC_FLAGS
+        cmd = [nvcc] + flags + EXTRA_DEFINES + ["-c", src, "-o", obj]
         proc = subprocess.run(cmd, capture_output=True, text=True)
         if proc.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, proc.stdout, proc.stderr))

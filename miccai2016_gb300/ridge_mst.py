@@ -102,13 +102,25 @@ def _local_mst_gpu(pts, vs, r, offsets, keep_device=False):
     """The local phase on the GPU (m16_ridge_mst_local, Boruvka rounds in the
     same (weight, i, j) order): the same edge set as _local_mst_host.  With
     keep_device, also the device points (int32 R x 3) and edges (int32 E x 2)."""
+    d_pts, d_edges = _local_mst_device(pts, vs, r, offsets)
+    e = d_edges.cpu().numpy().astype(np.int64)
+    if keep_device:
+        return e[:, 0], e[:, 1], d_pts, d_edges
+    return e[:, 0], e[:, 1]
+
+
+def _local_mst_device(pts, vs, r, offsets):
+    """_local_mst_gpu's device arrays: the points (int32 R x 3) and the
+    local forest's edges (int32 E x 2), nothing copied back."""
     torch = N.torch_mod()
     L = N.lib()
     R = len(pts)
-    lo = pts.min(0).astype(np.int32)
-    dims = (pts.max(0) - pts.min(0) + 1).astype(np.int32)
+    p32 = np.ascontiguousarray(pts, np.int32)
+    # per column: an axis-0 reduction of an R x 3 array is several times slower
+    lo = np.array([p32[:, k].min() for k in range(3)], np.int32)
+    dims = np.array([p32[:, k].max() for k in range(3)], np.int32) - lo + 1
     offs = np.ascontiguousarray(np.asarray(offsets, np.int32).reshape(-1, 3))
-    d_pts = torch.from_numpy(np.ascontiguousarray(pts, np.int32)).to(N.device())
+    d_pts = torch.from_numpy(p32).to(N.device())
     edges = torch.empty((max(R - 1, 1), 2), dtype=torch.int32, device=N.device())
     ws = N.workspace(L.m16_ridge_mst_workspace_bytes(R, dims.ctypes.data_as(ctypes.c_void_p), len(offs)))
     vsc = (ctypes.c_double * 3)(*[float(v) for v in vs])
@@ -118,10 +130,7 @@ def _local_mst_gpu(pts, vs, r, offsets, keep_device=False):
                                len(offs), float(r), N.ptr(edges), ctypes.byref(ne), N.ptr(ws), ws.numel(),
                                N.stream_ptr())
     N.check("m16_ridge_mst_local", st)
-    e = edges[:ne.value].cpu().numpy().astype(np.int64)
-    if keep_device:
-        return e[:, 0], e[:, 1], d_pts, edges[:ne.value]
-    return e[:, 0], e[:, 1]
+    return d_pts, edges[:ne.value]
 
 
 # pair evaluations above which the joins stay on the host (k-d trees)
@@ -170,7 +179,8 @@ def forest_components(n, ea, eb):
     return int(np.count_nonzero(starts)), comp
 
 
-def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, local="gpu", joins_on_device=True):
+def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, local="gpu", joins_on_device=True,
+                    on_device=False):
     """Edges (a, b) of the (weight, i, j)-ordered Euclidean MST of integer
     points (R x 3, axis order 0, 1, 2, distinct) with per-axis voxel size.
     With join_components=False only the local phase runs: the result is the
@@ -180,29 +190,46 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, lo
     default, or "host"); both give the same edges.  With the local phase on
     the GPU and unit voxel size, the trees are joined on the device too
     (m16_ridge_forest_joins, exact in integer arithmetic) unless
-    joins_on_device is False; otherwise k-d trees on the host join them."""
-    pts = np.asarray(points, dtype=np.int64)
+    joins_on_device is False; otherwise k-d trees on the host join them.
+    With on_device, where the edges are all known on the device (the local
+    phase there, and no joins or the device's) they stay there: (a, b) are
+    then CUDA int32 tensors; otherwise host int64 arrays."""
+    pts = np.asarray(points)
+    if pts.dtype.kind not in "iu":
+        pts = pts.astype(np.int64)
     R = len(pts)
     if R < 2:
         return np.zeros(0, np.int64), np.zeros(0, np.int64)
     vs = np.asarray(np.multiply(np.ones(3), voxel_size), np.float64)
-    u = np.multiply(pts, vs)   # the coordinates pdist sees
     r, offsets = _local_offsets(vs)
-    device = None
     if local == "gpu":
-        ta, tb, d_pts, d_edges = _local_mst_gpu(pts, vs, r, offsets, keep_device=True)
-        device = (d_pts, d_edges)
+        d_pts, d_edges = _local_mst_device(pts, vs, r, offsets)
+
+        def host_edges():
+            e = d_edges.cpu().numpy().astype(np.int64)
+            return e[:, 0], e[:, 1]
+
+        if not join_components or int(d_edges.shape[0]) == R - 1:   # not asked for, or already one tree
+            return (d_edges[:, 0].contiguous(), d_edges[:, 1].contiguous()) if on_device else host_edges()
+        if np.all(vs == 1.0) and joins_on_device:
+            j = _joins_gpu(d_pts, d_edges)
+            if j is not None:
+                if on_device:
+                    torch = N.torch_mod()
+                    up = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.int32)).to(d_edges.device)
+                    return torch.cat([d_edges[:, 0], up(j[0])]), torch.cat([d_edges[:, 1], up(j[1])])
+                ta, tb = host_edges()
+                return np.concatenate([ta, j[0]]), np.concatenate([tb, j[1]])
+        ta, tb = host_edges()
     elif local == "host":
+        pts = pts.astype(np.int64)
         ta, tb = _local_mst_host(pts, vs, r, offsets)
+        # global phase: join the local trees
+        if not join_components or len(ta) == R - 1:   # not asked for, or already one tree
+            return ta, tb
     else:
         raise ValueError("local must be 'gpu' or 'host'")
-    # global phase: join the local trees
-    if not join_components or len(ta) == R - 1:   # not asked for, or already one tree
-        return ta, tb
-    if device is not None and np.all(vs == 1.0) and joins_on_device:
-        j = _joins_gpu(*device)
-        if j is not None:
-            return np.concatenate([ta, j[0]]), np.concatenate([tb, j[1]])
+    u = np.multiply(pts.astype(np.int64), vs)   # the coordinates pdist sees (host joins only)
     ncomp, comp = forest_components(R, ta, tb)
     by_comp = np.argsort(comp, kind="stable")   # each component's points in index order
     members = np.split(by_comp, np.cumsum(np.bincount(comp, minlength=ncomp))[:-1])
@@ -316,7 +343,7 @@ def propagate_signs_device(d_dirs, edges_a, edges_b):
     n = int(d_dirs.shape[0])
     dev = d_dirs.device
     d_dirs = d_dirs.contiguous()
-    to_dev = lambda e: (e.to(device=dev, dtype=torch.int32) if N.is_torch(e)
+    to_dev = lambda e: (e.to(device=dev, dtype=torch.int32).contiguous() if N.is_torch(e)
                         else torch.from_numpy(np.ascontiguousarray(e, dtype=np.int32)).to(dev))
     d_a, d_b = to_dev(edges_a), to_dev(edges_b)
     ne = int(d_a.numel())
