@@ -1,4 +1,4 @@
-"""The sign propagation on the device (csrc/ridge_signs.cu through
+"""The sign propagation on the device (csrc/ridge_forest.cu through
 ridge_mst.propagate_signs_device): bit for bit the reference's
 point-by-point loop (adjust_directions.py:382-415) and the host propagation,
 on trees and forests with zero, near-zero (np.dot decides) and NaN dot
