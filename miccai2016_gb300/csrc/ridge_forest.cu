@@ -134,16 +134,16 @@ __global__ void rs_union_kernel(const int32_t *__restrict__ ea, const int32_t *_
     }
 }
 
-// root, parity to the root, and the lowest point of each piece
-__global__ void rs_flatten_kernel(uint32_t *parent, int64_t R, uint32_t *root, uint8_t *par, int32_t *piece_min,
-                                  unsigned long long *err)
+// root and parity to the root of every point.  A piece's root is also its
+// lowest point: a union links the higher root under the lower, so every
+// root is the least index of its tree (path halving moves no root).
+__global__ void rs_flatten_kernel(uint32_t *parent, int64_t R, uint32_t *root, uint8_t *par, unsigned long long *err)
 {
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < R; v += (int64_t)gridDim.x * blockDim.x) {
         uint32_t p;
         const uint32_t r = rs_find(parent, (uint32_t)v, &p, err);
         root[v] = r;
         par[v] = p ? 1 : 0;
-        atomicMin(piece_min + r, (int32_t)v);
     }
 }
 
@@ -151,7 +151,7 @@ __global__ void rs_flatten_kernel(uint32_t *parent, int64_t R, uint32_t *root, u
 // pieces' lowest points: (a, b, code, root a, root b, min a, min b)
 __global__ void rs_cut_kernel(const int32_t *__restrict__ ea, const int32_t *__restrict__ eb,
                               const int8_t *__restrict__ codes, int64_t n, int64_t R,
-                              const uint32_t *__restrict__ root, const int32_t *__restrict__ piece_min, int32_t *cut,
+                              const uint32_t *__restrict__ root, int32_t *cut,
                               unsigned long long *count, unsigned long long *bad)
 {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
@@ -169,8 +169,8 @@ __global__ void rs_cut_kernel(const int32_t *__restrict__ ea, const int32_t *__r
         o[2] = c;
         o[3] = (int32_t)ra;
         o[4] = (int32_t)rb;
-        o[5] = piece_min[ra];
-        o[6] = piece_min[rb];
+        o[5] = (int32_t)ra;   // the pieces' lowest points are their roots
+        o[6] = (int32_t)rb;
     }
 }
 
@@ -184,12 +184,11 @@ __global__ void rs_set_tops_kernel(const int32_t *__restrict__ set, int64_t n, i
 }
 
 // top of every other piece: its lowest point, with sign +1
-__global__ void rs_tops_kernel(const uint32_t *__restrict__ root, int64_t R, const int32_t *__restrict__ piece_min,
-                               int32_t *top, int8_t *top_sign)
+__global__ void rs_tops_kernel(const uint32_t *__restrict__ root, int64_t R, int32_t *top, int8_t *top_sign)
 {
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < R; v += (int64_t)gridDim.x * blockDim.x) {
         if (root[v] == (uint32_t)v && top[v] < 0) {
-            top[v] = piece_min[v];
+            top[v] = (int32_t)v;   // a root is its piece's lowest point
             top_sign[v] = 1;
         }
     }
@@ -208,7 +207,7 @@ __global__ void rs_signs_kernel(const uint32_t *__restrict__ root, const uint8_t
 }
 
 struct RsLayout {
-    size_t parent, root, par, pmin, top, tsign, cut, set, ctrl, total;
+    size_t parent, root, par, top, tsign, cut, set, ctrl, total;
 };
 
 RsLayout rs_layout(int64_t R, int64_t n_edges)
@@ -223,7 +222,6 @@ RsLayout rs_layout(int64_t R, int64_t n_edges)
     L.parent = take(4 * (size_t)R);
     L.root = take(4 * (size_t)R);
     L.par = take((size_t)R);
-    L.pmin = take(4 * (size_t)R);
     L.top = take(4 * (size_t)R);
     L.tsign = take((size_t)R);
     L.cut = take(28 * (size_t)std::max<int64_t>(n_edges, 1));
@@ -274,7 +272,6 @@ extern "C" int m16_ridge_signs(int64_t num_points, const int32_t *edges_a, const
     uint32_t *parent = (uint32_t *)(ws + Ly.parent);
     uint32_t *root = (uint32_t *)(ws + Ly.root);
     uint8_t *par = (uint8_t *)(ws + Ly.par);
-    int32_t *pmin = (int32_t *)(ws + Ly.pmin);
     int32_t *top = (int32_t *)(ws + Ly.top);
     int8_t *tsign = (int8_t *)(ws + Ly.tsign);
     int32_t *cut = (int32_t *)(ws + Ly.cut);
@@ -284,14 +281,13 @@ extern "C" int m16_ridge_signs(int64_t num_points, const int32_t *edges_a, const
     const int64_t R = num_points;
     const int gr = rs_grid(R), ge = rs_grid(std::max<int64_t>(num_edges, 1));
     M16_CUDA_TRY(cudaMemsetAsync(ctrl, 0, 32, st));
-    M16_CUDA_TRY(cudaMemsetAsync(pmin, 0x7f, 4 * (size_t)R, st));   // 0x7f7f7f7f > every index
     M16_CUDA_TRY(cudaMemsetAsync(top, 0xff, 4 * (size_t)R, st));    // -1: not set
     rs_init_kernel<<<gr, kRsBlock, 0, st>>>(parent, R);
     if (num_edges > 0)
         rs_union_kernel<<<ge, kRsBlock, 0, st>>>(edges_a, edges_b, codes, num_edges, R, parent, ctrl, ctrl + 2);
-    rs_flatten_kernel<<<gr, kRsBlock, 0, st>>>(parent, R, root, par, pmin, ctrl);
+    rs_flatten_kernel<<<gr, kRsBlock, 0, st>>>(parent, R, root, par, ctrl);
     if (num_edges > 0)
-        rs_cut_kernel<<<ge, kRsBlock, 0, st>>>(edges_a, edges_b, codes, num_edges, R, root, pmin, cut, ctrl + 1,
+        rs_cut_kernel<<<ge, kRsBlock, 0, st>>>(edges_a, edges_b, codes, num_edges, R, root, cut, ctrl + 1,
                                                ctrl + 2);
     M16_CUDA_TRY(cudaGetLastError());
     unsigned long long hc[3];
@@ -369,7 +365,7 @@ extern "C" int m16_ridge_signs(int64_t num_points, const int32_t *edges_a, const
         rs_set_tops_kernel<<<rs_grid(P), kRsBlock, 0, st>>>(set, P, top, tsign);
         M16_CUDA_TRY(cudaStreamSynchronize(st));   // hset goes out of scope
     }
-    rs_tops_kernel<<<gr, kRsBlock, 0, st>>>(root, R, pmin, top, tsign);
+    rs_tops_kernel<<<gr, kRsBlock, 0, st>>>(root, R, top, tsign);
     rs_signs_kernel<<<gr, kRsBlock, 0, st>>>(root, par, R, top, tsign, signs);
     M16_CUDA_TRY(cudaGetLastError());
     return M16_OK;
@@ -521,7 +517,7 @@ __global__ void fj_fill_kernel(unsigned long long *p, int64_t n)
 }
 
 struct FjLayout {
-    size_t parent, root, par, pmin, cid, comp, size, rank, start, fill, perm, bcount, chunks, key, ctrl, total;
+    size_t parent, root, par, cid, comp, size, rank, start, fill, perm, bcount, chunks, key, ctrl, total;
     int64_t max_keys, max_chunks;
 };
 
@@ -540,7 +536,6 @@ FjLayout fj_layout(int64_t R)
     L.parent = take(4 * (size_t)R);
     L.root = take(4 * (size_t)R);
     L.par = take((size_t)R);
-    L.pmin = take(4 * (size_t)R);
     L.cid = take(4 * (size_t)R);
     L.comp = take(4 * (size_t)R);
     L.size = take(4 * (size_t)R);
@@ -582,7 +577,6 @@ extern "C" int m16_ridge_forest_joins(const int32_t *pts3, int64_t num_points, c
     uint32_t *parent = (uint32_t *)(ws + Ly.parent);
     uint32_t *root = (uint32_t *)(ws + Ly.root);
     uint8_t *par = (uint8_t *)(ws + Ly.par);
-    int32_t *pmin = (int32_t *)(ws + Ly.pmin);
     int32_t *cid = (int32_t *)(ws + Ly.cid);
     int32_t *comp = (int32_t *)(ws + Ly.comp);
     unsigned *size = (unsigned *)(ws + Ly.size);
@@ -598,11 +592,10 @@ extern "C" int m16_ridge_forest_joins(const int32_t *pts3, int64_t num_points, c
     const int64_t nb = div_up(R, kFjScanItems);
     // components of the forest: union-find, each root its component's lowest point
     M16_CUDA_TRY(cudaMemsetAsync(ctrl, 0, 32, st));
-    M16_CUDA_TRY(cudaMemsetAsync(pmin, 0x7f, 4 * (size_t)R, st));
     rs_init_kernel<<<gr, kRsBlock, 0, st>>>(parent, R);
     if (num_edges > 0)
         rs_union_kernel<<<ge, kRsBlock, 0, st>>>(edges_a, edges_b, nullptr, num_edges, R, parent, ctrl, ctrl + 1);
-    rs_flatten_kernel<<<gr, kRsBlock, 0, st>>>(parent, R, root, par, pmin, ctrl);
+    rs_flatten_kernel<<<gr, kRsBlock, 0, st>>>(parent, R, root, par, ctrl);
     fj_root_count_kernel<<<(unsigned)nb, 256, 0, st>>>(root, R, bcount);
     M16_CUDA_TRY(cudaGetLastError());
     std::vector<unsigned> hb(nb);

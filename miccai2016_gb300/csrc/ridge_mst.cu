@@ -20,8 +20,18 @@
 // atomic minimum on the bits of a positive double, which order like the
 // values), then among the edges of that weight the least (i, j) packed into
 // 64 bits.
+//
+// Where every product point * voxel size is exact in double (unit voxel
+// size, or any size whose significand ends in at least as many zero bits as
+// the coordinates have bits), each difference u_i - u_j is exactly the offset
+// times the voxel size, so the weight depends on the offset alone (its sign
+// drops out in the squares): it is computed once per offset, with the same
+// operations, instead of once per candidate pair and pass -- the double
+// square root per pair was most of the local phase's time.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <float.h>
+#include <stdlib.h>
 
 #include <algorithm>
 #include <vector>
@@ -40,6 +50,7 @@ struct MstArgs {
     double r;
     const int *offs;       // n_off x 3, the candidate offsets (lexicographically positive)
     int n_off;
+    const double *offw;    // n_off: each offset's weight where it does not depend on the points, else null
     const int *grid;       // b0 x b1 x b2: point index or -1
     int *comp;             // R: component of each point (a root index)
     int *parent;           // R: for roots, the component hooked to
@@ -57,6 +68,18 @@ __device__ __forceinline__ double edge_weight(const MstArgs &a, int i, int j)
     const double d1 = __dsub_rn(__dmul_rn((double)a.pts[3 * i + 1], a.vs1), __dmul_rn((double)a.pts[3 * j + 1], a.vs1));
     const double d2 = __dsub_rn(__dmul_rn((double)a.pts[3 * i + 2], a.vs2), __dmul_rn((double)a.pts[3 * j + 2], a.vs2));
     return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
+}
+
+// the weight of every offset (edge_weight's operations on the offset times
+// the voxel size): where the products are exact this is every pair's weight
+__global__ void mst_offset_weights_kernel(MstArgs a, double *offw)
+{
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < a.n_off; o += gridDim.x * blockDim.x) {
+        const double d0 = __dmul_rn((double)a.offs[3 * o], a.vs0);
+        const double d1 = __dmul_rn((double)a.offs[3 * o + 1], a.vs1);
+        const double d2 = __dmul_rn((double)a.offs[3 * o + 2], a.vs2);
+        offw[o] = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
+    }
 }
 
 // the point grid; a point outside the box or a second point on one cell is
@@ -91,7 +114,7 @@ __global__ void mst_min_kernel(MstArgs a)
         const int lo = min(i, j), hi = max(i, j);
         const int ca = a.comp[lo], cb = a.comp[hi];
         if (ca == cb) continue;
-        const double w = edge_weight(a, lo, hi);
+        const double w = a.offw ? a.offw[o] : edge_weight(a, lo, hi);
         if (!(w <= a.r)) continue;
         const unsigned long long wb = (unsigned long long)__double_as_longlong(w);
         if (PASS == 0) {
@@ -156,7 +179,7 @@ __global__ void mst_reset_kernel(MstArgs a)
 }
 
 struct MstLayout {
-    size_t grid, comp, parent, minw, minij, offs, ctrl, total;
+    size_t grid, comp, parent, minw, minij, offs, offw, ctrl, total;
 };
 
 inline MstLayout mst_layout(int64_t R, int64_t cells, int n_off)
@@ -170,12 +193,28 @@ inline MstLayout mst_layout(int64_t R, int64_t cells, int n_off)
     L.minw = take((size_t)R * 8);
     L.minij = take((size_t)R * 8);
     L.offs = take((size_t)std::max(n_off, 1) * 12);
+    L.offw = take((size_t)std::max(n_off, 1) * 8);
     L.ctrl = take(24);
     L.total = off;
     return L;
 }
 
 inline int blocks_for(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(16 * kSMs, div_up(n, 256))); }
+
+// whether p * v is exact in double for every integer |p| <= maxabs: v's
+// significand (53 bits) ends in at least as many zero bits as maxabs has
+inline bool products_exact(double v, int64_t maxabs)
+{
+    if (!(v >= DBL_MIN) || !isfinite(v)) return false;
+    int e = 0;
+    const double m = frexp(v, &e);                        // v = m * 2^e, m in [0.5, 1)
+    const uint64_t sig = (uint64_t)ldexp(m, 53);          // the 53-bit significand, exactly
+    int tz = 0;
+    while (tz < 53 && !((sig >> tz) & 1u)) ++tz;
+    int bits = 0;
+    while (bits < 63 && (maxabs >> bits) != 0) ++bits;
+    return bits <= tz;
+}
 
 }  // namespace
 }  // namespace m16
@@ -218,6 +257,7 @@ extern "C" int m16_ridge_mst_local(const int32_t *pts3, int64_t num_points, cons
     a.r = r;
     a.offs = (const int *)(ws + L.offs);
     a.n_off = n_offsets;
+    a.offw = nullptr;
     a.grid = (const int *)(ws + L.grid);
     a.comp = (int *)(ws + L.comp);
     a.parent = (int *)(ws + L.parent);
@@ -227,6 +267,18 @@ extern "C" int m16_ridge_mst_local(const int32_t *pts3, int64_t num_points, cons
     a.ctrl = (unsigned long long *)(ws + L.ctrl);
     if (n_offsets > 0)
         M16_CUDA_TRY(cudaMemcpyAsync(ws + L.offs, offsets3, (size_t)n_offsets * 12, cudaMemcpyHostToDevice, st));
+    // the largest coordinate magnitude in the box and in the offsets
+    int64_t maxabs = 0;
+    for (int k = 0; k < 3; ++k) {
+        maxabs = std::max<int64_t>(maxabs, std::llabs((int64_t)box_lo3[k]));
+        maxabs = std::max<int64_t>(maxabs, std::llabs((int64_t)box_lo3[k] + box_dims3[k] - 1));
+    }
+    for (int64_t o = 0; o < 3 * (int64_t)n_offsets; ++o) maxabs = std::max<int64_t>(maxabs, std::llabs((int64_t)offsets3[o]));
+    if (n_offsets > 0 && products_exact(voxel_size3[0], maxabs) && products_exact(voxel_size3[1], maxabs) &&
+        products_exact(voxel_size3[2], maxabs)) {
+        mst_offset_weights_kernel<<<1, 256, 0, st>>>(a, (double *)(ws + L.offw));
+        a.offw = (const double *)(ws + L.offw);
+    }
     M16_CUDA_TRY(cudaMemsetAsync(ws + L.grid, 0xff, (size_t)cells * 4, st));
     M16_CUDA_TRY(cudaMemsetAsync(a.ctrl, 0, 24, st));
     mst_grid_kernel<<<blocks_for(num_points), 256, 0, st>>>(a, (int *)(ws + L.grid));
