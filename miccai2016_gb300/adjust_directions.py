@@ -247,8 +247,9 @@ class AdvancedAdjuster(TreePrintable):
         if len(coords) == 0:
             raise ValueError("no ridge points: nothing to propagate directions along")
         with self._timed("mst_local" if not join_components else "mst_local_and_joins"):
+            shape = tuple(int(v) for v in self.response.shape)
             a, b = ridge_mst_edges(coords, self.voxel_size, join_components=join_components, local=self.mst_local,
-                                   on_device=True)
+                                   on_device=True, d_points=d_coords, box=((0, 0, 0), shape))
         with self._timed("sign_propagation"):
             d_dirs = d_main[d_coords[:, 0], d_coords[:, 1], d_coords[:, 2]]
             adjusted = propagate_signs_device(d_dirs, a, b).cpu().numpy()

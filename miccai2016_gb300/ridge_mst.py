@@ -109,18 +109,28 @@ def _local_mst_gpu(pts, vs, r, offsets, keep_device=False):
     return e[:, 0], e[:, 1]
 
 
-def _local_mst_device(pts, vs, r, offsets):
+def _local_mst_device(pts, vs, r, offsets, d_points=None, box=None):
     """_local_mst_gpu's device arrays: the points (int32 R x 3) and the
-    local forest's edges (int32 E x 2), nothing copied back."""
+    local forest's edges (int32 E x 2), nothing copied back.  d_points: the
+    same points already on the device (any integer dtype); box: (lo, dims)
+    of a box holding them (else their bounding box, from the host points)."""
     torch = N.torch_mod()
     L = N.lib()
     R = len(pts)
-    p32 = np.ascontiguousarray(pts, np.int32)
-    # per column: an axis-0 reduction of an R x 3 array is several times slower
-    lo = np.array([p32[:, k].min() for k in range(3)], np.int32)
-    dims = np.array([p32[:, k].max() for k in range(3)], np.int32) - lo + 1
+    if d_points is not None:
+        d_pts = d_points.to(device=N.device(), dtype=torch.int32).contiguous()
+    else:
+        p32 = np.ascontiguousarray(pts, np.int32)
+        d_pts = torch.from_numpy(p32).to(N.device())
+    if box is not None:
+        lo = np.ascontiguousarray(box[0], np.int32)
+        dims = np.ascontiguousarray(box[1], np.int32)
+    else:
+        p32 = np.ascontiguousarray(pts, np.int32)
+        # per column: an axis-0 reduction of an R x 3 array is several times slower
+        lo = np.array([p32[:, k].min() for k in range(3)], np.int32)
+        dims = np.array([p32[:, k].max() for k in range(3)], np.int32) - lo + 1
     offs = np.ascontiguousarray(np.asarray(offsets, np.int32).reshape(-1, 3))
-    d_pts = torch.from_numpy(p32).to(N.device())
     edges = torch.empty((max(R - 1, 1), 2), dtype=torch.int32, device=N.device())
     ws = N.workspace(L.m16_ridge_mst_workspace_bytes(R, dims.ctypes.data_as(ctypes.c_void_p), len(offs)))
     vsc = (ctypes.c_double * 3)(*[float(v) for v in vs])
@@ -180,7 +190,7 @@ def forest_components(n, ea, eb):
 
 
 def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, local="gpu", joins_on_device=True,
-                    on_device=False):
+                    on_device=False, d_points=None, box=None):
     """Edges (a, b) of the (weight, i, j)-ordered Euclidean MST of integer
     points (R x 3, axis order 0, 1, 2, distinct) with per-axis voxel size.
     With join_components=False only the local phase runs: the result is the
@@ -193,7 +203,10 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, lo
     joins_on_device is False; otherwise k-d trees on the host join them.
     With on_device, where the edges are all known on the device (the local
     phase there, and no joins or the device's) they stay there: (a, b) are
-    then CUDA int32 tensors; otherwise host int64 arrays."""
+    then CUDA int32 tensors; otherwise host int64 arrays.  d_points (the
+    same points as a CUDA tensor) and box ((lo, dims) of a box holding them,
+    e.g. the volume's) spare the local phase on the GPU its upload and its
+    bounding box; a point outside the box fails the call."""
     pts = np.asarray(points)
     if pts.dtype.kind not in "iu":
         pts = pts.astype(np.int64)
@@ -203,7 +216,7 @@ def ridge_mst_edges(points, voxel_size=(1.0, 1.0, 1.0), join_components=True, lo
     vs = np.asarray(np.multiply(np.ones(3), voxel_size), np.float64)
     r, offsets = _local_offsets(vs)
     if local == "gpu":
-        d_pts, d_edges = _local_mst_device(pts, vs, r, offsets)
+        d_pts, d_edges = _local_mst_device(pts, vs, r, offsets, d_points=d_points, box=box)
 
         def host_edges():
             e = d_edges.cpu().numpy().astype(np.int64)
